@@ -1,0 +1,112 @@
+"""Named workloads.
+
+The reference's compiled-in presets (src/app.rs:354-360, setups/*.yaml) and
+the synthetic circumbinary-disk workloads this implementation is measured on.
+The synthetic disks extend the reference's InfiniteDisk initial model with a
+low-density cavity and seeded noise; the choices the workload descriptions
+leave open (buffer rate and scale, domain radius of the larger meshes, cavity
+profile) are fixed here once and used everywhere.
+"""
+import random
+from typing import List, Tuple
+
+from .config import DiskModel, Euler, Isothermal, Mesh, Physics
+
+CAVITY = dict(cavity_radius=2.5, cavity_floor=1e-4)
+NOISE = 1e-3
+
+
+def iso_physics(q: float = 1.0, e: float = 0.0, nu: float = 1e-3) -> Physics:
+    """Isothermal circumbinary physics: softening 0.05, sink radius 0.05,
+    sink rate 10, PLM θ = 1.5, RK2, CFL 0.4, buffer as in iso-circular
+    (setups/iso-circular.yaml:17-19)."""
+    return Physics(buffer_rate=1000.0, buffer_scale=0.3, binary_eccentricity=e, binary_mass_ratio=q,
+                   cfl=0.4, plm=1.5, rk_order="RK2", sink_radius=0.05, sink_rate=10.0,
+                   viscosity=("constant_nu", nu), softening_length=0.05)
+
+
+def iso_disk(num_blocks: int, block_size: int, seed: int = 1, mach: float = 10.0, q: float = 1.0,
+             e: float = 0.0, nu: float = 1e-3, domain_radius: float = 8.0):
+    """An isothermal disk: Σ = 1 with a cavity r < 2.5a, Keplerian velocity,
+    ±1e-3 multiplicative Σ noise."""
+    mesh = Mesh(num_blocks=num_blocks, block_size=block_size, domain_radius=domain_radius)
+    hydro = Isothermal(mach_number=mach)
+    physics = iso_physics(q=q, e=e, nu=nu)
+    model = DiskModel(surface_density=1.0, noise=NOISE, seed=seed, **CAVITY)
+    return mesh, hydro, physics, model
+
+
+def disk_512(seed: int = 1):
+    """Plain FP64 isothermal run: 8×8 blocks of 64² zones (512²), half-width 8a."""
+    return iso_disk(8, 64, seed=seed)
+
+
+def disk_2048(seed: int = 1):
+    """The same disk on 16×16 blocks of 128² zones (2048²)."""
+    return iso_disk(16, 128, seed=seed)
+
+
+def euler_beta_disk(num_blocks: int = 32, block_size: int = 128, seed: int = 3):
+    """Euler disk with β-cooling (β = 10), α-viscosity 0.1, q = 0.5, e = 0.5,
+    γ = 5/3, model Mach 10 (4096² by default)."""
+    mesh = Mesh(num_blocks=num_blocks, block_size=block_size, domain_radius=8.0)
+    hydro = Euler(gamma_law_index=5.0 / 3.0, cooling_coefficient=0.0, cooling_beta=10.0)
+    physics = Physics(buffer_rate=1000.0, buffer_scale=0.3, binary_eccentricity=0.5, binary_mass_ratio=0.5,
+                      cfl=0.4, plm=1.5, rk_order="RK2", sink_radius=0.05, sink_rate=10.0,
+                      viscosity=("alpha", 0.1), softening_length=0.05)
+    model = DiskModel(surface_density=1.0, mach_number=10.0, noise=NOISE, seed=seed, **CAVITY)
+    return mesh, hydro, physics, model
+
+
+def sweep(nruns: int = 64, seed: int = 4):
+    """Batched parameter sweep: grid side drawn from {256, 512, 768, 1024} in
+    64² blocks, q ~ U[0.1, 1], e ~ U[0, 0.8], Mach ~ U[10, 40],
+    ν ~ U[1e-4, 1e-3]."""
+    rng = random.Random(seed)
+    out = []
+    for k in range(nruns):
+        side = rng.choice([256, 512, 768, 1024])
+        q = rng.uniform(0.1, 1.0)
+        e = rng.uniform(0.0, 0.8)
+        mach = rng.uniform(10.0, 40.0)
+        nu = rng.uniform(1e-4, 1e-3)
+        out.append(iso_disk(side // 64, 64, seed=seed * 1000 + k, mach=mach, q=q, e=e, nu=nu))
+    return out
+
+
+def disk_8192(seed: int = 5):
+    """Single large isothermal run, q = 1, e = 0.1, 64×64 blocks of 128²."""
+    return iso_disk(64, 128, seed=seed, e=0.1)
+
+
+# ----------------------------------------------------------------------------
+# The reference's compiled-in presets (src/app.rs:354-360), as data.
+REFERENCE_PRESETS = {
+    "iso-circular": dict(
+        model=("infinite_disk", dict(mach_number=None, surface_density=1.0)),
+        hydro=Isothermal(mach_number=10.0),
+        mesh=Mesh(block_size=64, num_blocks=6, domain_radius=12.0),
+        physics=Physics(binary_eccentricity=0.0, binary_mass_ratio=1.0, buffer_rate=1000.0, buffer_scale=0.3,
+                        cfl=0.3, plm=1.8, rk_order="RK2", nu=0.001, sink_radius=0.05, sink_rate=1.0),
+        control=dict(num_orbits=100, checkpoint_interval=1.0, time_series_interval=None, fold=10,
+                     num_threads=None, output_directory="data"),
+    ),
+    "cooling-cbd": dict(
+        model=("infinite_disk", dict(mach_number=10.0, surface_density=1.0)),
+        hydro=Euler(gamma_law_index=1.666, cooling_coefficient=1e3, pressure_floor=1e-16),
+        mesh=Mesh(block_size=64, num_blocks=12, domain_radius=12.0),
+        physics=Physics(binary_eccentricity=0.0, binary_mass_ratio=1.0, buffer_rate=1000.0, buffer_scale=1.0,
+                        cfl=0.3, nu=0.001, plm=1.8, rk_order="RK2", sink_radius=0.05, sink_rate=1.0),
+        control=dict(num_orbits=100, checkpoint_interval=1.0, time_series_interval=0.01, fold=10,
+                     num_threads=None, output_directory="data"),
+    ),
+    "test-grid-visc": dict(
+        model=("infinite_disk", dict(mach_number=None)),
+        hydro=Isothermal(mach_number=10.0),
+        mesh=Mesh(block_size=64, num_blocks=6, domain_radius=12.0),
+        physics=Physics(binary_eccentricity=0.0, binary_mass_ratio=1.0, buffer_rate=1000.0, buffer_scale=0.3,
+                        cfl=0.3, plm=1.8, rk_order="RK2", nu=0.0, sink_radius=0.1, sink_rate=1.0, one_body=True),
+        control=dict(num_orbits=100, checkpoint_interval=1.0, time_series_interval=0.01, fold=10,
+                     num_threads=None, output_directory="data"),
+    ),
+}

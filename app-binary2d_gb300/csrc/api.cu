@@ -1,0 +1,916 @@
+// api.cu — the C ABI of include/b2d.h: contexts, state transfer, and the
+// advance driver (the role of scheme::advance, src/scheme.rs:323-349).
+//
+// Built with --fmad=false: the Kepler solve and the time bookkeeping of the
+// prologue kernel round exactly like the FP64 CPU restatement.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "runtime.cuh"
+
+namespace b2d {
+cudaError_t launch_stage_f64(int nf, const StageArgs& a, int grid, int tw, size_t smem, cudaStream_t s);
+cudaError_t launch_stage_f32(int nf, int store, const StageArgs& a, int grid, int tw, size_t smem, cudaStream_t s);
+void host_block_vertices(const b2d_config* c, int b, double* xv);
+void host_cell_centers(const b2d_config* c, int b, double* xc);
+}  // namespace b2d
+
+using namespace b2d;
+
+static thread_local std::string g_last_error;
+
+static b2d_status fail(b2d_status s, const std::string& msg)
+{
+    g_last_error = msg;
+    return s;
+}
+
+#define CUDA_TRY(expr)                                                                              \
+    do {                                                                                            \
+        cudaError_t e_ = (expr);                                                                    \
+        if (e_ != cudaSuccess)                                                                      \
+            return fail(B2D_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_));          \
+    } while (0)
+
+extern "C" const char* b2d_last_error(void) { return g_last_error.c_str(); }
+
+// ---------------------------------------------------------------------------
+// Device kernels of the runtime.
+
+// Two-body orbit at time t: OrbitalElements::orbital_state_from_time
+// (kepler-two-body, restated; called at physics.rs:419-421).  Elements
+// (a, M, q, e) = (1, 1, q, e), or (1e-12, 1, 1, 0) for one_body
+// (physics.rs:411-417).  Periapsis on +x at t = 0; Newton iteration on
+// Kepler's equation E - e sin E = n t from E = n t.
+__device__ void kepler_orbit(const RunDev& rd, double t, double* o)
+{
+    double a, M, q, e;
+    if (rd.p.one_body) { a = 1e-12; M = 1.0; q = 1.0; e = 0.0; }
+    else { a = 1.0; M = 1.0; q = rd.binary_q; e = rd.binary_e; }
+    double n = sqrt(M / (a * a * a));
+    double mean = n * t;
+    double E = mean;
+    for (int k = 0; k < 64; ++k) {
+        double f = E - e * sin(E) - mean;
+        if (fabs(f) < 1e-15) break;
+        E = E - f / (1.0 - e * cos(E));
+    }
+    double cE = cos(E), sE = sin(E);
+    double b = sqrt(1.0 - e * e);
+    double x = a * (cE - e);
+    double y = a * b * sE;
+    double edot = n / (1.0 - e * cE);
+    double vx = -a * sE * edot;
+    double vy = a * b * cE * edot;
+    double m1 = M / (1.0 + q);
+    double m2 = M * q / (1.0 + q);
+    double f1 = m2 / M, f2 = m1 / M;
+    o[0] = m1; o[1] = -x * f1; o[2] = -y * f1; o[3] = -vx * f1; o[4] = -vy * f1;
+    o[5] = m2; o[6] = x * f2; o[7] = y * f2; o[8] = vx * f2; o[9] = vy * f2;
+}
+
+// Start of an advance, one CTA per run: dt = cfl·dx / max signal speed
+// (floored by dt_min, scheme.rs:336-340), the stage times of all `fold` RK
+// steps (try_advance_rk stamps t + dt, scheme.rs:168-170; weighted_average
+// averages time, state.rs:213-214), and the binary at each stage time.
+__global__ void prologue_kernel(const RunDev* runs, int fold, int rk, int start, int final_slot)
+{
+    const RunDev& rd = runs[blockIdx.x];
+    const int stages = rk;
+    if (threadIdx.x == 0) {
+        double amax = __longlong_as_double((long long)*rd.amax);
+        double dt = rd.p.cfl * rd.p.dx / amax;
+        if (rd.p.has_dt_min) dt = fmax(dt, rd.p.dt_min);
+        *rd.dt = dt;
+        *rd.amax = 0ull;
+        double t = rd.time[start];
+        int s = 0;
+        for (int f = 0; f < fold; ++f) {
+            const double t0 = t;
+            if (rk == 1) {
+                rd.stage_time[s++] = t0;
+                t = t0 + dt;
+            } else if (rk == 2) {
+                rd.stage_time[s++] = t0;
+                double t1 = t0 + dt;
+                rd.stage_time[s++] = t1;
+                double t2 = t1 + dt;
+                t = t2 * (-0.5 + 1.) + t0 * 0.5;
+            } else {
+                rd.stage_time[s++] = t0;
+                double t1 = t0 + dt;
+                rd.stage_time[s++] = t1;
+                double t2 = t1 + dt;
+                double t2a = t2 * (-0.75 + 1.) + t0 * 0.75;
+                rd.stage_time[s++] = t2a;
+                double t3 = t2a + dt;
+                const double bf = 1.0 / 3.0;
+                t = t3 * (-bf + 1.) + t0 * bf;
+            }
+        }
+        rd.time[final_slot] = t;
+        rd.iter[final_slot] = rd.iter[start] + fold;
+    }
+    __syncthreads();
+    for (int s = threadIdx.x; s < fold * stages; s += blockDim.x) kepler_orbit(rd, rd.stage_time[s], rd.orbit + 10 * s);
+}
+
+// State::max_signal_speed (state.rs:121-133) of one run's slot.
+template <int NF, int STORE>
+__global__ void max_speed_kernel(const RunDev* runs, int run, int slot)
+{
+    const RunDev& rd = runs[run];
+    const size_t nn = (size_t)rd.N * rd.N;
+    double a = 0.0;
+    for (size_t z = blockIdx.x * (size_t)blockDim.x + threadIdx.x; z < nn; z += (size_t)gridDim.x * blockDim.x) {
+        double u[NF];
+        for (int f = 0; f < NF; ++f) {
+            if (STORE == 0) u[f] = ((const double*)rd.slot[slot])[f * nn + z];
+            else {
+                const float* p = (const float*)rd.slot[slot];
+                u[f] = (double)p[(2 * f) * nn + z] + (double)p[(2 * f + 1) * nn + z];
+            }
+        }
+        a = fmax(max_signal_speed<NF, double>(rd.p, u), a);
+    }
+    __shared__ double red[256];
+    red[threadIdx.x] = a;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0 && red[0] > 0.0) atomicMax(rd.amax, (unsigned long long)__double_as_longlong(red[0]));
+}
+
+// Block layout [nb][nb][bs][bs][nf] (host) <-> field planes (device).
+__device__ __forceinline__ size_t block_index(int gi, int gj, int bs, int nb, int nf)
+{
+    int bi = gi / bs, bj = gj / bs, li = gi % bs, lj = gj % bs;
+    return ((((size_t)bi * nb + bj) * bs + li) * bs + lj) * nf;
+}
+
+__global__ void scatter_kernel(const double* src, void* dst, int N, int bs, int nb, int nf, int store)
+{
+    const size_t nn = (size_t)N * N;
+    for (size_t z = blockIdx.x * (size_t)blockDim.x + threadIdx.x; z < nn; z += (size_t)gridDim.x * blockDim.x) {
+        int gi = (int)(z / N), gj = (int)(z % N);
+        size_t b = block_index(gi, gj, bs, nb, nf);
+        for (int f = 0; f < nf; ++f) {
+            double v = src[b + f];
+            if (store == 0) ((double*)dst)[f * nn + z] = v;
+            else {
+                float hi = (float)v;
+                float lo = (float)(v - (double)hi);
+                ((float*)dst)[(2 * f) * nn + z] = hi;
+                ((float*)dst)[(2 * f + 1) * nn + z] = lo;
+            }
+        }
+    }
+}
+
+__global__ void gather_kernel(const void* src, double* dst, int N, int bs, int nb, int nf, int store)
+{
+    const size_t nn = (size_t)N * N;
+    for (size_t z = blockIdx.x * (size_t)blockDim.x + threadIdx.x; z < nn; z += (size_t)gridDim.x * blockDim.x) {
+        int gi = (int)(z / N), gj = (int)(z % N);
+        size_t b = block_index(gi, gj, bs, nb, nf);
+        for (int f = 0; f < nf; ++f) {
+            double v;
+            if (store == 0) v = ((const double*)src)[f * nn + z];
+            else v = (double)((const float*)src)[(2 * f) * nn + z] + (double)((const float*)src)[(2 * f + 1) * nn + z];
+            dst[b + f] = v;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Host-side context.
+
+namespace {
+
+struct RunHost {
+    b2d_config cfg;
+    int N, bs, nb, nblocks;
+    size_t state_bytes;
+    void* slot[NSLOTS] = {};
+    void* bg = nullptr;
+    double* ledger[NSLOTS] = {};
+    double* partial = nullptr;
+    unsigned* counter = nullptr;
+    double *xc = nullptr, *xv = nullptr;
+    float *xcf = nullptr, *xvf = nullptr;
+    double* stage_time = nullptr;
+    double* orbit = nullptr;
+};
+
+// Host mirror of the per-context control block in device memory.
+struct Control {
+    b2d_error err;
+    int pad_[2];
+};
+
+struct StagePlan {
+    int in, base, out;
+    double bf;
+};
+
+}  // namespace
+
+struct b2d_ctx {
+    int nruns = 0, nf = 3, precision = 0, hydro = 0, rk = 2;
+    int tw = 64, th = 64;
+    int cur = 0;
+    std::vector<RunHost> runs;
+    std::vector<RunDev> rdev_h;
+    RunDev* rdev = nullptr;
+    // control arrays (device)
+    double* d_dt = nullptr;           // [nruns]
+    double* d_time = nullptr;         // [nruns][NSLOTS]
+    long long* d_iter = nullptr;      // [nruns][NSLOTS]
+    unsigned long long* d_amax = nullptr;  // [nruns]
+    b2d_error* d_err = nullptr;
+    double* d_staging = nullptr;
+    size_t staging_bytes = 0;
+    int max_stages = 0;
+    cudaStream_t stream = nullptr;
+    bool use_graphs = true;
+    std::map<std::pair<int, int>, cudaGraphExec_t> graphs;
+    long long launches = 0;
+    int total_tiles = 0;
+    int pending_final = -1;
+    // instrumentation
+    bool instrument = false;
+    std::vector<cudaEvent_t> ev;
+    double stage_ms_total = 0.0;
+    long long stage_count = 0;
+};
+
+static int rsize_of(int precision) { return precision == B2D_PREC_FP64 ? 8 : 4; }
+
+static size_t stage_smem_bytes(int nf, int rsize, int tw)
+{
+    int cw = 3 * nf + 4;
+    size_t elems = 4 * (size_t)(tw + 4) * nf + 3 * (size_t)(tw + 2) * cw + 2 * (size_t)(tw + 1) * nf;
+    size_t bytes = elems * rsize;
+    size_t red = (size_t)tw * 8;
+    return std::max(bytes, red);
+}
+
+static DevParams make_params(const b2d_config& c)
+{
+    DevParams p;
+    memset(&p, 0, sizeof p);
+    p.hydro = c.hydro_kind;
+    p.visc = c.viscosity_kind;
+    p.sink_model = c.sink_model;
+    p.one_body = c.one_body;
+    p.has_mach_ceiling = c.has_mach_ceiling;
+    p.has_density_floor = c.has_density_floor;
+    p.has_pressure_floor = c.has_pressure_floor;
+    p.density_index = c.density_index;
+    p.cooling_kind = c.cooling_kind;
+    p.cooling_slow_start = c.cooling_slow_start;
+    p.has_dt_min = c.has_dt_min;
+    double block_length = 2.0 * c.domain_radius / (double)c.num_blocks;  // mesh.rs:27-29
+    p.dx = block_length / (double)c.block_size;                          // mesh.rs:86-88
+    p.inv_dx = 1.0 / p.dx;
+    p.cfl = c.cfl;
+    p.dt_min = c.dt_min;
+    p.plm = c.plm;
+    p.pdt = c.has_plm_density_trigger ? c.plm_density_trigger : 0.0;     // scheme.rs:216-220
+    p.nu = c.viscosity;
+    p.lambda = c.lambda_multiplier;
+    p.mach2 = c.mach_number * c.mach_number;
+    p.gamma = c.hydro_kind == B2D_EULER ? c.gamma_law_index : 1.0;        // physics.rs:477-479
+    p.gm1 = p.gamma - 1.0;
+    p.sqrt_gm = sqrt(p.gamma);
+    double s = c.has_softening_length ? c.softening_length : c.sink_radius;  // physics.rs:399-405
+    p.soft2 = s * s;
+    p.sink_r2 = c.sink_radius * c.sink_radius;
+    p.sink_rate = c.sink_rate;
+    p.domain_radius = c.domain_radius;
+    p.buffer_scale = c.buffer_scale;
+    p.half_buffer_rate = 0.5 * c.buffer_rate;
+    double q = c.one_body ? 1.0 : c.binary_mass_ratio;
+    double m1 = 1.0 / (1.0 + q), m2 = 1.0 * q / (1.0 + q);
+    double R = c.domain_radius;
+    p.omega_outer = sqrt((m1 + m2) / (R * R * R));                        // physics.rs:445
+    p.fake_thr = c.fake_mass_threshold;
+    p.fake_rate = c.fake_mass_rate;
+    p.density_floor = c.density_floor;
+    p.pressure_floor = c.pressure_floor;
+    p.density_floor_pow_gamma = c.has_density_floor ? pow(c.density_floor, p.gamma) : 0.0;
+    p.mach_ceiling2 = c.mach_ceiling * c.mach_ceiling;
+    p.cool_coef = c.cooling_coefficient;
+    p.cool_beta = c.cooling_beta;
+    return p;
+}
+
+static b2d_status validate(const b2d_config& c, int hydro, int rk)
+{
+    if (c.num_blocks < 1 || c.block_size < 1) return fail(B2D_ERR_INVALID, "num_blocks and block_size must be positive");
+    if (c.hydro_kind != hydro) return fail(B2D_ERR_INVALID, "all runs of a context must share the hydro kind");
+    if (c.rk_order != rk) return fail(B2D_ERR_INVALID, "all runs of a context must share rk_order");
+    if (rk < 1 || rk > 3) return fail(B2D_ERR_INVALID, "rk_order must be 1, 2 or 3");
+    long long N = (long long)c.num_blocks * c.block_size;
+    if (N * N > (1ll << 31)) return fail(B2D_ERR_INVALID, "mesh too large (more than 2^31 zones per run)");
+    if (!(c.domain_radius > 0)) return fail(B2D_ERR_INVALID, "domain_radius must be positive");
+    return B2D_OK;
+}
+
+static int default_tile_w(int bs)
+{
+    for (int w : {128, 64, 32})
+        if (bs % w == 0) return w;
+    return bs;
+}
+
+static bool tile_ok(const b2d_ctx* ctx, int tw, int th)
+{
+    if (tw < 1 || th < 1 || tw > 256) return false;
+    for (const RunHost& r : ctx->runs)
+        if (r.bs % tw || r.bs % th) return false;
+    if (tw % 32 != 0) {
+        // a partial warp is allowed only when it is the whole block width
+        for (const RunHost& r : ctx->runs)
+            if (r.bs != tw) return false;
+    }
+    return true;
+}
+
+static void free_ctx(b2d_ctx* ctx)
+{
+    if (!ctx) return;
+    for (auto& kv : ctx->graphs) cudaGraphExecDestroy(kv.second);
+    for (RunHost& r : ctx->runs) {
+        for (int s = 0; s < NSLOTS; ++s) { cudaFree(r.slot[s]); cudaFree(r.ledger[s]); }
+        cudaFree(r.bg); cudaFree(r.partial); cudaFree(r.counter);
+        cudaFree(r.xc); cudaFree(r.xv); cudaFree(r.xcf); cudaFree(r.xvf);
+        cudaFree(r.stage_time); cudaFree(r.orbit);
+    }
+    cudaFree(ctx->rdev); cudaFree(ctx->d_dt); cudaFree(ctx->d_time); cudaFree(ctx->d_iter);
+    cudaFree(ctx->d_amax); cudaFree(ctx->d_err); cudaFree(ctx->d_staging);
+    for (cudaEvent_t e : ctx->ev) cudaEventDestroy(e);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+// Rebuild the tile bookkeeping for the current tile shape and push the run
+// descriptors to the device.
+static b2d_status sync_rundev(b2d_ctx* ctx)
+{
+    int base = 0;
+    for (int i = 0; i < ctx->nruns; ++i) {
+        RunHost& r = ctx->runs[i];
+        RunDev& d = ctx->rdev_h[i];
+        d.tiles_i = r.N / ctx->th;
+        d.tiles_j = r.N / ctx->tw;
+        d.ntiles = d.tiles_i * d.tiles_j;
+        d.tile_base = base;
+        d.tiles_per_block = (r.bs / ctx->th) * (r.bs / ctx->tw);
+        base += d.ntiles;
+        CUDA_TRY(cudaFree(r.partial));
+        r.partial = nullptr;
+        CUDA_TRY(cudaMalloc(&r.partial, sizeof(double) * r.nblocks * d.tiles_per_block * NITEMS * ctx->nf));
+        d.partial = r.partial;
+    }
+    ctx->total_tiles = base;
+    CUDA_TRY(cudaMemcpy(ctx->rdev, ctx->rdev_h.data(), sizeof(RunDev) * ctx->nruns, cudaMemcpyHostToDevice));
+    for (auto& kv : ctx->graphs) cudaGraphExecDestroy(kv.second);
+    ctx->graphs.clear();
+    return B2D_OK;
+}
+
+static b2d_status ensure_stage_capacity(b2d_ctx* ctx, int fold)
+{
+    int need = fold * ctx->rk;
+    if (need <= ctx->max_stages) return B2D_OK;
+    int cap = std::max(need, 64);
+    for (int i = 0; i < ctx->nruns; ++i) {
+        RunHost& r = ctx->runs[i];
+        CUDA_TRY(cudaFree(r.stage_time));
+        CUDA_TRY(cudaFree(r.orbit));
+        r.stage_time = nullptr;
+        r.orbit = nullptr;
+        CUDA_TRY(cudaMalloc(&r.stage_time, sizeof(double) * cap));
+        CUDA_TRY(cudaMalloc(&r.orbit, sizeof(double) * 10 * cap));
+        ctx->rdev_h[i].stage_time = r.stage_time;
+        ctx->rdev_h[i].orbit = r.orbit;
+    }
+    ctx->max_stages = cap;
+    CUDA_TRY(cudaMemcpy(ctx->rdev, ctx->rdev_h.data(), sizeof(RunDev) * ctx->nruns, cudaMemcpyHostToDevice));
+    for (auto& kv : ctx->graphs) cudaGraphExecDestroy(kv.second);
+    ctx->graphs.clear();
+    return B2D_OK;
+}
+
+extern "C" b2d_ctx* b2d_create(const b2d_config* cfgs, int32_t nruns, int32_t precision, b2d_status* status)
+{
+    b2d_status st_dummy;
+    if (!status) status = &st_dummy;
+    if (!cfgs || nruns < 1) { *status = fail(B2D_ERR_INVALID, "need at least one run"); return nullptr; }
+    if (precision < 0 || precision > 2) { *status = fail(B2D_ERR_INVALID, "bad precision"); return nullptr; }
+    int ndev = 0;
+    cudaError_t ce = cudaGetDeviceCount(&ndev);
+    if (ce != cudaSuccess || ndev == 0) {
+        *status = fail(B2D_ERR_CUDA, std::string("no CUDA device: ") + cudaGetErrorString(ce));
+        return nullptr;
+    }
+    b2d_ctx* ctx = new b2d_ctx;
+    ctx->nruns = nruns;
+    ctx->precision = precision;
+    ctx->hydro = cfgs[0].hydro_kind;
+    ctx->rk = cfgs[0].rk_order;
+    ctx->nf = ctx->hydro == B2D_EULER ? 4 : 3;
+    int wsize = precision == B2D_PREC_FP32_COMP ? 8 : (precision == B2D_PREC_FP64 || precision == B2D_PREC_FP32_STATE64 ? 8 : 8);
+    int min_bs = 1 << 30;
+    for (int i = 0; i < nruns; ++i) {
+        b2d_status v = validate(cfgs[i], ctx->hydro, ctx->rk);
+        if (v != B2D_OK) { *status = v; free_ctx(ctx); return nullptr; }
+        min_bs = std::min(min_bs, cfgs[i].block_size);
+    }
+#define CREATE_TRY(expr)                                                                         \
+    do {                                                                                         \
+        cudaError_t e_ = (expr);                                                                 \
+        if (e_ != cudaSuccess) {                                                                 \
+            *status = fail(B2D_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_));    \
+            free_ctx(ctx);                                                                       \
+            return nullptr;                                                                      \
+        }                                                                                        \
+    } while (0)
+    CREATE_TRY(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+    CREATE_TRY(cudaMalloc(&ctx->rdev, sizeof(RunDev) * nruns));
+    CREATE_TRY(cudaMalloc(&ctx->d_dt, sizeof(double) * nruns));
+    CREATE_TRY(cudaMalloc(&ctx->d_time, sizeof(double) * nruns * NSLOTS));
+    CREATE_TRY(cudaMalloc(&ctx->d_iter, sizeof(long long) * nruns * NSLOTS));
+    CREATE_TRY(cudaMalloc(&ctx->d_amax, sizeof(unsigned long long) * nruns));
+    CREATE_TRY(cudaMalloc(&ctx->d_err, sizeof(b2d_error)));
+    CREATE_TRY(cudaMemset(ctx->d_time, 0, sizeof(double) * nruns * NSLOTS));
+    CREATE_TRY(cudaMemset(ctx->d_iter, 0, sizeof(long long) * nruns * NSLOTS));
+    CREATE_TRY(cudaMemset(ctx->d_amax, 0, sizeof(unsigned long long) * nruns));
+    CREATE_TRY(cudaMemset(ctx->d_err, 0, sizeof(b2d_error)));
+    CREATE_TRY(cudaMemset(ctx->d_dt, 0, sizeof(double) * nruns));
+
+    ctx->runs.resize(nruns);
+    ctx->rdev_h.resize(nruns);
+    const int store = precision == B2D_PREC_FP32_COMP ? 1 : 0;
+    (void)wsize;
+    for (int i = 0; i < nruns; ++i) {
+        RunHost& r = ctx->runs[i];
+        RunDev& d = ctx->rdev_h[i];
+        memset(&d, 0, sizeof d);
+        r.cfg = cfgs[i];
+        r.bs = cfgs[i].block_size;
+        r.nb = cfgs[i].num_blocks;
+        r.N = r.bs * r.nb;
+        r.nblocks = r.nb * r.nb;
+        size_t nn = (size_t)r.N * r.N;
+        r.state_bytes = store == 1 ? nn * ctx->nf * 2 * sizeof(float) : nn * ctx->nf * sizeof(double);
+        for (int s = 0; s < NSLOTS; ++s) {
+            CREATE_TRY(cudaMalloc(&r.slot[s], r.state_bytes));
+            CREATE_TRY(cudaMemset(r.slot[s], 0, r.state_bytes));
+            CREATE_TRY(cudaMalloc(&r.ledger[s], sizeof(double) * r.nblocks * NITEMS * ctx->nf));
+            CREATE_TRY(cudaMemset(r.ledger[s], 0, sizeof(double) * r.nblocks * NITEMS * ctx->nf));
+        }
+        CREATE_TRY(cudaMalloc(&r.bg, r.state_bytes));
+        CREATE_TRY(cudaMemset(r.bg, 0, r.state_bytes));
+        CREATE_TRY(cudaMalloc(&r.counter, sizeof(unsigned) * r.nblocks));
+        CREATE_TRY(cudaMemset(r.counter, 0, sizeof(unsigned) * r.nblocks));
+        // geometry tables
+        std::vector<double> xc(r.N), xv((size_t)r.nb * (r.bs + 1));
+        for (int b = 0; b < r.nb; ++b) {
+            host_cell_centers(&cfgs[i], b, xc.data() + (size_t)b * r.bs);
+            host_block_vertices(&cfgs[i], b, xv.data() + (size_t)b * (r.bs + 1));
+        }
+        std::vector<float> xcf(xc.begin(), xc.end()), xvf(xv.begin(), xv.end());
+        CREATE_TRY(cudaMalloc(&r.xc, sizeof(double) * xc.size()));
+        CREATE_TRY(cudaMalloc(&r.xv, sizeof(double) * xv.size()));
+        CREATE_TRY(cudaMalloc(&r.xcf, sizeof(float) * xc.size()));
+        CREATE_TRY(cudaMalloc(&r.xvf, sizeof(float) * xv.size()));
+        CREATE_TRY(cudaMemcpy(r.xc, xc.data(), sizeof(double) * xc.size(), cudaMemcpyHostToDevice));
+        CREATE_TRY(cudaMemcpy(r.xv, xv.data(), sizeof(double) * xv.size(), cudaMemcpyHostToDevice));
+        CREATE_TRY(cudaMemcpy(r.xcf, xcf.data(), sizeof(float) * xc.size(), cudaMemcpyHostToDevice));
+        CREATE_TRY(cudaMemcpy(r.xvf, xvf.data(), sizeof(float) * xv.size(), cudaMemcpyHostToDevice));
+
+        d.N = r.N; d.bs = r.bs; d.nb = r.nb; d.nblocks = r.nblocks;
+        d.xc = r.xc; d.xv = r.xv; d.xcf = r.xcf; d.xvf = r.xvf;
+        for (int s = 0; s < NSLOTS; ++s) { d.slot[s] = r.slot[s]; d.ledger[s] = r.ledger[s]; }
+        d.bg = r.bg;
+        d.time = ctx->d_time + (size_t)i * NSLOTS;
+        d.iter = ctx->d_iter + (size_t)i * NSLOTS;
+        d.counter = r.counter;
+        d.dt = ctx->d_dt + i;
+        d.amax = ctx->d_amax + i;
+        d.binary_q = cfgs[i].binary_mass_ratio;
+        d.binary_e = cfgs[i].binary_eccentricity;
+        d.p = make_params(cfgs[i]);
+        ctx->staging_bytes = std::max(ctx->staging_bytes, nn * ctx->nf * sizeof(double));
+    }
+    CREATE_TRY(cudaMalloc(&ctx->d_staging, ctx->staging_bytes));
+    ctx->tw = default_tile_w(min_bs);
+    ctx->th = std::min(64, min_bs);
+    while (!tile_ok(ctx, ctx->tw, ctx->th) && ctx->th > 1) ctx->th /= 2;
+    if (!tile_ok(ctx, ctx->tw, ctx->th)) {
+        *status = fail(B2D_ERR_INVALID, "runs of a context need a common tile shape (block sizes must share a divisor)");
+        free_ctx(ctx);
+        return nullptr;
+    }
+    if (sync_rundev(ctx) != B2D_OK) { *status = B2D_ERR_CUDA; free_ctx(ctx); return nullptr; }
+    if (ensure_stage_capacity(ctx, 16) != B2D_OK) { *status = B2D_ERR_CUDA; free_ctx(ctx); return nullptr; }
+    *status = B2D_OK;
+    return ctx;
+#undef CREATE_TRY
+}
+
+extern "C" void b2d_destroy(b2d_ctx* ctx)
+{
+    if (ctx) cudaStreamSynchronize(ctx->stream);
+    free_ctx(ctx);
+}
+
+extern "C" int32_t b2d_num_fields(const b2d_ctx* ctx) { return ctx ? ctx->nf : 0; }
+
+static int store_of(const b2d_ctx* ctx) { return ctx->precision == B2D_PREC_FP32_COMP ? 1 : 0; }
+
+static b2d_status launch_max_speed(b2d_ctx* ctx, int run, int slot)
+{
+    CUDA_TRY(cudaMemsetAsync(ctx->d_amax + run, 0, sizeof(unsigned long long), ctx->stream));
+    int grid = 4 * 152;
+    if (ctx->nf == 3) {
+        if (store_of(ctx) == 0) max_speed_kernel<3, 0><<<grid, 256, 0, ctx->stream>>>(ctx->rdev, run, slot);
+        else max_speed_kernel<3, 1><<<grid, 256, 0, ctx->stream>>>(ctx->rdev, run, slot);
+    } else {
+        if (store_of(ctx) == 0) max_speed_kernel<4, 0><<<grid, 256, 0, ctx->stream>>>(ctx->rdev, run, slot);
+        else max_speed_kernel<4, 1><<<grid, 256, 0, ctx->stream>>>(ctx->rdev, run, slot);
+    }
+    ctx->launches++;
+    CUDA_TRY(cudaGetLastError());
+    return B2D_OK;
+}
+
+extern "C" b2d_status b2d_upload_state(b2d_ctx* ctx, int32_t run, const double* cons, const double* background,
+                                       const double* ledger, double time, int64_t iteration_num, int64_t iteration_den)
+{
+    if (!ctx || run < 0 || run >= ctx->nruns || !cons) return fail(B2D_ERR_INVALID, "bad arguments");
+    if (iteration_den != 1) return fail(B2D_ERR_INVALID, "iteration must be an integer at step boundaries");
+    RunHost& r = ctx->runs[run];
+    size_t n = (size_t)r.N * r.N * ctx->nf;
+    int store = store_of(ctx);
+    int grid = 4 * 152;
+    CUDA_TRY(cudaMemcpyAsync(ctx->d_staging, cons, n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    scatter_kernel<<<grid, 256, 0, ctx->stream>>>(ctx->d_staging, r.slot[ctx->cur], r.N, r.bs, r.nb, ctx->nf, store);
+    ctx->launches++;
+    CUDA_TRY(cudaGetLastError());
+    if (background) {
+        CUDA_TRY(cudaMemcpyAsync(ctx->d_staging, background, n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+        scatter_kernel<<<grid, 256, 0, ctx->stream>>>(ctx->d_staging, r.bg, r.N, r.bs, r.nb, ctx->nf, store);
+        ctx->launches++;
+        CUDA_TRY(cudaGetLastError());
+    }
+    size_t nled = (size_t)r.nblocks * NITEMS * ctx->nf;
+    if (ledger) CUDA_TRY(cudaMemcpyAsync(r.ledger[ctx->cur], ledger, nled * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    else CUDA_TRY(cudaMemsetAsync(r.ledger[ctx->cur], 0, nled * sizeof(double), ctx->stream));
+    long long it = iteration_num;
+    CUDA_TRY(cudaMemcpyAsync(ctx->d_time + (size_t)run * NSLOTS + ctx->cur, &time, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    CUDA_TRY(cudaMemcpyAsync(ctx->d_iter + (size_t)run * NSLOTS + ctx->cur, &it, sizeof(long long), cudaMemcpyHostToDevice, ctx->stream));
+    b2d_status s = launch_max_speed(ctx, run, ctx->cur);
+    if (s != B2D_OK) return s;
+    CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return B2D_OK;
+}
+
+extern "C" b2d_status b2d_upload_conserved(b2d_ctx* ctx, int32_t run, const double* cons)
+{
+    if (!ctx || run < 0 || run >= ctx->nruns || !cons) return fail(B2D_ERR_INVALID, "bad arguments");
+    RunHost& r = ctx->runs[run];
+    size_t n = (size_t)r.N * r.N * ctx->nf;
+    CUDA_TRY(cudaMemcpyAsync(ctx->d_staging, cons, n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    scatter_kernel<<<4 * 152, 256, 0, ctx->stream>>>(ctx->d_staging, r.slot[ctx->cur], r.N, r.bs, r.nb, ctx->nf, store_of(ctx));
+    ctx->launches++;
+    CUDA_TRY(cudaGetLastError());
+    b2d_status s = launch_max_speed(ctx, run, ctx->cur);
+    if (s != B2D_OK) return s;
+    CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return B2D_OK;
+}
+
+extern "C" b2d_status b2d_download_state(b2d_ctx* ctx, int32_t run, double* cons, double* time, int64_t* iteration_num,
+                                         int64_t* iteration_den)
+{
+    if (!ctx || run < 0 || run >= ctx->nruns) return fail(B2D_ERR_INVALID, "bad arguments");
+    RunHost& r = ctx->runs[run];
+    size_t n = (size_t)r.N * r.N * ctx->nf;
+    if (cons) {
+        gather_kernel<<<4 * 152, 256, 0, ctx->stream>>>(r.slot[ctx->cur], ctx->d_staging, r.N, r.bs, r.nb, ctx->nf, store_of(ctx));
+        ctx->launches++;
+        CUDA_TRY(cudaGetLastError());
+        CUDA_TRY(cudaMemcpyAsync(cons, ctx->d_staging, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    double t = 0;
+    long long it = 0;
+    CUDA_TRY(cudaMemcpyAsync(&t, ctx->d_time + (size_t)run * NSLOTS + ctx->cur, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    CUDA_TRY(cudaMemcpyAsync(&it, ctx->d_iter + (size_t)run * NSLOTS + ctx->cur, sizeof(long long), cudaMemcpyDeviceToHost, ctx->stream));
+    CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    if (time) *time = t;
+    if (iteration_num) *iteration_num = it;
+    if (iteration_den) *iteration_den = 1;
+    return B2D_OK;
+}
+
+extern "C" b2d_status b2d_download_ledger(b2d_ctx* ctx, int32_t run, double* ledger)
+{
+    if (!ctx || run < 0 || run >= ctx->nruns || !ledger) return fail(B2D_ERR_INVALID, "bad arguments");
+    RunHost& r = ctx->runs[run];
+    size_t nled = (size_t)r.nblocks * NITEMS * ctx->nf;
+    CUDA_TRY(cudaMemcpyAsync(ledger, r.ledger[ctx->cur], nled * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return B2D_OK;
+}
+
+extern "C" b2d_status b2d_max_signal_speed(b2d_ctx* ctx, int32_t run, double* out)
+{
+    if (!ctx || run < 0 || run >= ctx->nruns || !out) return fail(B2D_ERR_INVALID, "bad arguments");
+    unsigned long long bits = 0;
+    CUDA_TRY(cudaMemcpyAsync(&bits, ctx->d_amax + run, sizeof bits, cudaMemcpyDeviceToHost, ctx->stream));
+    CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    double v;
+    memcpy(&v, &bits, sizeof v);
+    *out = v;
+    return B2D_OK;
+}
+
+// ---------------------------------------------------------------------------
+// The advance.
+
+static int free_slot(int a, int b, int c)
+{
+    for (int s = 0; s < NSLOTS; ++s)
+        if (s != a && s != b && s != c) return s;
+    return -1;
+}
+
+// Slot schedule of `fold` RK steps from slot `start`, which is left intact.
+static std::vector<StagePlan> plan_advance(int rk, int fold, int start, int* final_slot)
+{
+    std::vector<StagePlan> plan;
+    int base = start;
+    for (int f = 0; f < fold; ++f) {
+        if (rk == 1) {
+            int a = free_slot(start, base, -1);
+            plan.push_back({base, -1, a, 0.0});
+            base = a;
+        } else if (rk == 2) {
+            int a = free_slot(start, base, -1);
+            plan.push_back({base, -1, a, 0.0});
+            int b = free_slot(start, base, a);
+            plan.push_back({a, base, b, 0.5});
+            base = b;
+        } else {
+            int a = free_slot(start, base, -1);
+            plan.push_back({base, -1, a, 0.0});
+            int b = free_slot(start, base, a);
+            plan.push_back({a, base, b, 0.75});
+            int c = free_slot(start, base, b);
+            plan.push_back({b, base, c, 1.0 / 3.0});
+            base = c;
+        }
+    }
+    *final_slot = base;
+    return plan;
+}
+
+static df32w split_df(double v)
+{
+    float hi = (float)v;
+    float lo = (float)(v - (double)hi);
+    return {hi, lo};
+}
+
+static b2d_status launch_stage(b2d_ctx* ctx, const StagePlan& sp, int stage, int amax_flag)
+{
+    StageArgs a;
+    a.runs = ctx->rdev;
+    a.nruns = ctx->nruns;
+    a.th = ctx->th;
+    a.in_slot = sp.in;
+    a.base_slot = sp.base;
+    a.out_slot = sp.out;
+    a.stage = stage;
+    a.amax_flag = amax_flag;
+    a.bf = sp.bf;
+    a.w1f = split_df(-sp.bf + 1.0);
+    a.bff = split_df(sp.bf);
+    a.err = ctx->d_err;
+    size_t smem = stage_smem_bytes(ctx->nf, rsize_of(ctx->precision), ctx->tw);
+    cudaError_t e;
+    if (ctx->precision == B2D_PREC_FP64) e = launch_stage_f64(ctx->nf, a, ctx->total_tiles, ctx->tw, smem, ctx->stream);
+    else e = launch_stage_f32(ctx->nf, store_of(ctx), a, ctx->total_tiles, ctx->tw, smem, ctx->stream);
+    if (e != cudaSuccess) return fail(B2D_ERR_CUDA, std::string("stage kernel launch: ") + cudaGetErrorString(e));
+    return B2D_OK;
+}
+
+static b2d_status enqueue_advance(b2d_ctx* ctx, int fold, int start, int* final_slot, bool count)
+{
+    std::vector<StagePlan> plan = plan_advance(ctx->rk, fold, start, final_slot);
+    prologue_kernel<<<ctx->nruns, 32, 0, ctx->stream>>>(ctx->rdev, fold, ctx->rk, start, *final_slot);
+    CUDA_TRY(cudaGetLastError());
+    if (count) ctx->launches++;
+    for (size_t s = 0; s < plan.size(); ++s) {
+        bool timed = ctx->instrument;
+        if (timed) {
+            while (ctx->ev.size() < 2 * plan.size()) {
+                cudaEvent_t e;
+                CUDA_TRY(cudaEventCreate(&e));
+                ctx->ev.push_back(e);
+            }
+            CUDA_TRY(cudaEventRecord(ctx->ev[2 * s], ctx->stream));
+        }
+        b2d_status st = launch_stage(ctx, plan[s], (int)s, s + 1 == plan.size());
+        if (st != B2D_OK) return st;
+        if (timed) CUDA_TRY(cudaEventRecord(ctx->ev[2 * s + 1], ctx->stream));
+        if (count) ctx->launches++;
+    }
+    return B2D_OK;
+}
+
+static b2d_status run_advance(b2d_ctx* ctx, int fold, int* final_slot)
+{
+    b2d_status st = ensure_stage_capacity(ctx, fold);
+    if (st != B2D_OK) return st;
+    const int start = ctx->cur;
+    if (!ctx->use_graphs || ctx->instrument) {
+        st = enqueue_advance(ctx, fold, start, final_slot, true);
+        if (st != B2D_OK) return st;
+        if (ctx->instrument) {
+            CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+            for (int s = 0; s < fold * ctx->rk; ++s) {
+                float ms = 0;
+                CUDA_TRY(cudaEventElapsedTime(&ms, ctx->ev[2 * s], ctx->ev[2 * s + 1]));
+                ctx->stage_ms_total += ms;
+                ctx->stage_count++;
+            }
+        }
+        return B2D_OK;
+    }
+    auto key = std::make_pair(fold, start);
+    auto it = ctx->graphs.find(key);
+    if (it == ctx->graphs.end()) {
+        cudaGraph_t g;
+        CUDA_TRY(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        st = enqueue_advance(ctx, fold, start, final_slot, false);
+        cudaError_t ec = cudaStreamEndCapture(ctx->stream, &g);
+        if (st != B2D_OK) return st;
+        if (ec != cudaSuccess) return fail(B2D_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ec));
+        cudaGraphExec_t ge;
+        CUDA_TRY(cudaGraphInstantiate(&ge, g, 0));
+        cudaGraphDestroy(g);
+        it = ctx->graphs.emplace(key, ge).first;
+    } else {
+        plan_advance(ctx->rk, fold, start, final_slot);
+    }
+    CUDA_TRY(cudaGraphLaunch(it->second, ctx->stream));
+    ctx->launches += 1 + (long long)fold * ctx->rk;
+    return B2D_OK;
+}
+
+static b2d_status finish_advance(b2d_ctx* ctx, int start, int final_slot, double* dt_out, b2d_error* err_out)
+{
+    b2d_error err;
+    CUDA_TRY(cudaMemcpyAsync(&err, ctx->d_err, sizeof err, cudaMemcpyDeviceToHost, ctx->stream));
+    std::vector<double> dts(ctx->nruns);
+    CUDA_TRY(cudaMemcpyAsync(dts.data(), ctx->d_dt, sizeof(double) * ctx->nruns, cudaMemcpyDeviceToHost, ctx->stream));
+    CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    if (dt_out) memcpy(dt_out, dts.data(), sizeof(double) * ctx->nruns);
+    if (err.code != 0) {
+        if (err_out) *err_out = err;
+        CUDA_TRY(cudaMemsetAsync(ctx->d_err, 0, sizeof(b2d_error), ctx->stream));
+        ctx->cur = start;
+        for (int r = 0; r < ctx->nruns; ++r) {
+            b2d_status s = launch_max_speed(ctx, r, start);
+            if (s != B2D_OK) return s;
+        }
+        CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+        return fail((b2d_status)err.code, "hydro error during advance");
+    }
+    ctx->cur = final_slot;
+    return B2D_OK;
+}
+
+extern "C" b2d_status b2d_advance(b2d_ctx* ctx, int32_t fold, double* dt_out, b2d_error* err_out)
+{
+    if (!ctx || fold < 1) return fail(B2D_ERR_INVALID, "bad arguments");
+    const int start = ctx->cur;
+    int final_slot = -1;
+    b2d_status st = run_advance(ctx, fold, &final_slot);
+    if (st != B2D_OK) return st;
+    return finish_advance(ctx, start, final_slot, dt_out, err_out);
+}
+
+extern "C" b2d_status b2d_advance_async(b2d_ctx* ctx, int32_t fold)
+{
+    if (!ctx || fold < 1) return fail(B2D_ERR_INVALID, "bad arguments");
+    int final_slot = -1;
+    b2d_status st = run_advance(ctx, fold, &final_slot);
+    if (st != B2D_OK) return st;
+    ctx->cur = final_slot;
+    return B2D_OK;
+}
+
+extern "C" b2d_status b2d_synchronize(b2d_ctx* ctx, double* dt_out, b2d_error* err_out)
+{
+    if (!ctx) return fail(B2D_ERR_INVALID, "bad arguments");
+    return finish_advance(ctx, ctx->cur, ctx->cur, dt_out, err_out);
+}
+
+extern "C" b2d_status b2d_set_tile(b2d_ctx* ctx, int32_t tile_w, int32_t tile_h)
+{
+    if (!ctx) return fail(B2D_ERR_INVALID, "bad arguments");
+    int tw = tile_w ? tile_w : ctx->tw, th = tile_h ? tile_h : ctx->th;
+    if (!tile_ok(ctx, tw, th)) return fail(B2D_ERR_INVALID, "tile must divide the block size (width a multiple of 32, at most 256)");
+    CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    ctx->tw = tw;
+    ctx->th = th;
+    return sync_rundev(ctx);
+}
+
+extern "C" b2d_status b2d_get_tile(const b2d_ctx* ctx, int32_t* tile_w, int32_t* tile_h)
+{
+    if (!ctx) return fail(B2D_ERR_INVALID, "bad arguments");
+    if (tile_w) *tile_w = ctx->tw;
+    if (tile_h) *tile_h = ctx->th;
+    return B2D_OK;
+}
+
+extern "C" b2d_status b2d_set_graphs(b2d_ctx* ctx, int32_t enable)
+{
+    if (!ctx) return fail(B2D_ERR_INVALID, "bad arguments");
+    ctx->use_graphs = enable != 0;
+    return B2D_OK;
+}
+
+extern "C" int64_t b2d_launch_count(const b2d_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+extern "C" int64_t b2d_launches_per_advance(const b2d_ctx* ctx, int32_t fold)
+{
+    return ctx ? 1 + (int64_t)fold * ctx->rk : 0;
+}
+
+extern "C" b2d_status b2d_set_instrument(b2d_ctx* ctx, int32_t enable)
+{
+    if (!ctx) return fail(B2D_ERR_INVALID, "bad arguments");
+    ctx->instrument = enable != 0;
+    ctx->stage_ms_total = 0.0;
+    ctx->stage_count = 0;
+    return B2D_OK;
+}
+
+extern "C" b2d_status b2d_stage_stats(const b2d_ctx* ctx, int64_t* count, double* total_ms)
+{
+    if (!ctx) return fail(B2D_ERR_INVALID, "bad arguments");
+    if (count) *count = ctx->stage_count;
+    if (total_ms) *total_ms = ctx->stage_ms_total;
+    return B2D_OK;
+}
+
+extern "C" b2d_status b2d_time_stages(b2d_ctx* ctx, int32_t fold, int32_t reps, double* ms_per_stage)
+{
+    if (!ctx || fold < 1 || reps < 1 || !ms_per_stage) return fail(B2D_ERR_INVALID, "bad arguments");
+    bool was = ctx->instrument;
+    b2d_set_instrument(ctx, 1);
+    for (int r = 0; r < reps; ++r) {
+        int fs;
+        b2d_status st = run_advance(ctx, fold, &fs);
+        if (st != B2D_OK) { ctx->instrument = was; return st; }
+        ctx->cur = fs;
+    }
+    *ms_per_stage = ctx->stage_count ? ctx->stage_ms_total / ctx->stage_count : 0.0;
+    ctx->instrument = was;
+    return B2D_OK;
+}
+
+extern "C" b2d_status b2d_stream(const b2d_ctx* ctx, void** stream)
+{
+    if (!ctx || !stream) return fail(B2D_ERR_INVALID, "bad arguments");
+    *stream = (void*)ctx->stream;
+    return B2D_OK;
+}
+
+extern "C" b2d_status b2d_pin_host(void* ptr, uint64_t bytes)
+{
+    CUDA_TRY(cudaHostRegister(ptr, bytes, cudaHostRegisterDefault));
+    return B2D_OK;
+}
+
+extern "C" b2d_status b2d_unpin_host(void* ptr)
+{
+    CUDA_TRY(cudaHostUnregister(ptr));
+    return B2D_OK;
+}

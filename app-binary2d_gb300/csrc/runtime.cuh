@@ -1,0 +1,49 @@
+// runtime.cuh — device-side descriptors shared by the kernels and the C ABI.
+#pragma once
+
+#include "../../include/b2d.h"
+#include "physics.cuh"
+
+namespace b2d {
+
+constexpr int NSLOTS = 4;  // state slots: the advance input is kept intact until success
+
+struct df32w { float hi, lo; };
+
+// One run of a batch as the kernels see it.
+struct RunDev {
+    int N, bs, nb, nblocks;
+    int tiles_i, tiles_j, ntiles, tile_base;
+    int tiles_per_block, pad_;
+    const double* xc;        // [N] cell centres by global index (block formula, mesh.rs:49-54)
+    const double* xv;        // [nb][bs+1] block vertices (mesh.rs:42-47)
+    const float* xcf;
+    const float* xvf;
+    void* slot[NSLOTS];      // conserved state per slot (STORE layout)
+    const void* bg;          // BlockData::initial_conserved (STORE layout)
+    double* ledger[NSLOTS];  // [nblocks][7][nf] per slot
+    double* time;            // [NSLOTS]
+    long long* iter;         // [NSLOTS]
+    double* partial;         // [nblocks][tiles_per_block][7 nf]
+    unsigned* counter;       // [nblocks]
+    double* dt;              // [1]
+    double* stage_time;      // [max_stages]
+    double* orbit;           // [max_stages][10]: m, x, y, vx, vy of body 1 then body 2
+    unsigned long long* amax;
+    double binary_q, binary_e;
+    DevParams p;
+};
+
+struct StageArgs {
+    const RunDev* runs;
+    int nruns;
+    int th;
+    int in_slot, base_slot, out_slot;
+    int stage;
+    int amax_flag;
+    double bf;               // weight of the RK base state (br of godunov-core)
+    b2d::df32w w1f, bff;     // 1 - bf and bf as double-float
+    b2d_error* err;
+};
+
+}  // namespace b2d

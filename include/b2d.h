@@ -1,0 +1,259 @@
+/*
+ * b2d.h — C ABI of the GB300 implementation of binary2d's explicit
+ * finite-volume Runge–Kutta step on the block mesh.
+ *
+ * Drop-in boundary.  The reference exposes the step as the Rust generic
+ *
+ *     scheme::advance<H: Hydrodynamics>(state: State<H::Conserved>, hydro: H,
+ *         mesh: &Mesh, physics: &Physics, fold: usize, timestep: &mut f64,
+ *         block_data: &HashMap<BlockIndex, BlockData<C>>, runtime: &Runtime)
+ *         -> Result<State<C>, HydroError>                    (src/scheme.rs:323-349)
+ *
+ * called once per loop iteration by main.rs:run (src/main.rs:159-167).  The
+ * functions below replace that call: a context owns the device copy of the
+ * `State` (conserved fields, time, iteration, per-block source ledger) and of
+ * the `BlockData` background (scheme.rs:36-58), and b2d_advance() performs
+ * `fold` Runge–Kutta steps with one dt computed at the start, exactly as
+ * scheme::advance does.
+ *
+ * Conventions
+ *  - Plain C types only; every buffer argument is caller-owned host memory
+ *    unless the name says `device`.
+ *  - Conserved arrays use the reference's block layout
+ *    [num_blocks][num_blocks][block_size][block_size][nf], blocks in
+ *    mesh.block_indexes() order (src/mesh.rs:84-89: i outer, j inner), zones
+ *    row-major within a block (i ↔ x, j ↔ y, j contiguous), nf = 3 for
+ *    isothermal (Σ, Σvx, Σvy) and 4 for Euler (Σ, Σvx, Σvy, E).
+ *  - Source ledgers (ItemizedChange, src/state.rs:27-36) use
+ *    [num_blocks][num_blocks][7][nf] with items ordered sink1, sink2, grav1,
+ *    grav2, buffer, cooling, fake_mass.
+ *  - A context is not thread-safe: one host thread drives it, as main.rs
+ *    drives scheme::advance from one thread.
+ *  - No C++ exception crosses this boundary; every call returns a b2d_status.
+ *  - There is no CPU fallback: without a usable CUDA device b2d_create fails
+ *    with B2D_ERR_CUDA.
+ */
+#ifndef B2D_H
+#define B2D_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------------ */
+/* Status codes.  The hydro errors mirror HydroErrorType (src/physics.rs:25-36). */
+typedef enum b2d_status {
+    B2D_OK                 = 0,
+    B2D_ERR_NEG_DENSITY    = 1,  /* HydroErrorType::NegativeDensity            */
+    B2D_ERR_NEG_PRESSURE   = 2,  /* HydroErrorType::NegativePressure           */
+    B2D_ERR_UNBOUND_ORBIT  = 3,  /* HydroErrorType::OrbitalEvolutionError      */
+    B2D_ERR_TIMEOUT        = 4,  /* a bounded device wait gave up               */
+    B2D_ERR_CUDA           = 5,  /* CUDA runtime error (message via b2d_last_error) */
+    B2D_ERR_INVALID        = 6,  /* bad argument                                */
+    B2D_ERR_UNSUPPORTED    = 7   /* option combination not built                */
+} b2d_status;
+
+/* Hydro systems, AnyHydro (src/app.rs:28-33). */
+enum { B2D_ISOTHERMAL = 0, B2D_EULER = 1 };
+
+/* Arithmetic of the stage kernels. */
+enum {
+    B2D_PREC_FP64        = 0,  /* FP64 stencil, FP64 state: parity path                */
+    B2D_PREC_FP32_STATE64 = 1, /* FP32 stencil, FP64 state                             */
+    B2D_PREC_FP32_COMP   = 2   /* FP32 stencil, FP32 state + FP32 compensation word    */
+};
+
+/* ViscosityModel (src/physics.rs:97-103), SinkModel (src/physics.rs:109-115). */
+enum { B2D_VISC_CONSTANT_NU = 0, B2D_VISC_ALPHA = 1 };
+enum { B2D_SINK_IMPARTIAL = 0, B2D_SINK_TORQUE_FREE = 1 };
+
+/* Euler cooling law: the reference's T^4 law (src/physics.rs:701-738), or
+ * β-cooling, which has no counterpart in the reference (a new option). */
+enum { B2D_COOLING_T4 = 0, B2D_COOLING_BETA = 1 };
+
+/*
+ * Run configuration: Mesh (src/mesh.rs:19-33), the Isothermal / Euler hydro
+ * parameters (src/physics.rs:256-303) and Physics (src/physics.rs:121-218)
+ * flattened into one plain struct.  Optional fields of the reference
+ * (Option<f64>) carry a has_* flag.  The deprecated aliases nu / alpha /
+ * lambda (physics.rs:211-230) are resolved by the host before filling this.
+ */
+typedef struct b2d_config {
+    /* Mesh */
+    int32_t num_blocks;
+    int32_t block_size;
+    double  domain_radius;
+
+    /* Hydro */
+    int32_t hydro_kind;            /* B2D_ISOTHERMAL | B2D_EULER            */
+    int32_t density_index;         /* Euler, default 2                      */
+    double  mach_number;           /* Isothermal                            */
+    double  gamma_law_index;       /* Euler                                 */
+    double  cooling_coefficient;   /* Euler, T^4 law                        */
+    double  pressure_floor;        /* Euler, valid if has_pressure_floor    */
+    double  density_floor;         /* valid if has_density_floor            */
+    int32_t has_pressure_floor;
+    int32_t has_density_floor;
+    int32_t cooling_slow_start;    /* Euler                                 */
+    int32_t cooling_kind;          /* B2D_COOLING_T4 | B2D_COOLING_BETA     */
+    double  cooling_beta;          /* β of β-cooling                        */
+
+    /* Physics */
+    double  buffer_rate;
+    double  buffer_scale;
+    double  binary_eccentricity;
+    double  binary_mass_ratio;
+    double  lambda_multiplier;
+    double  viscosity;             /* ν or α, per viscosity_kind            */
+    int32_t viscosity_kind;        /* B2D_VISC_*                            */
+    int32_t sink_model;            /* B2D_SINK_*                            */
+    double  cfl;
+    double  plm;
+    double  plm_density_trigger;   /* valid if has_plm_density_trigger      */
+    double  fake_mass_threshold;
+    double  fake_mass_rate;
+    double  mach_ceiling;          /* valid if has_mach_ceiling             */
+    double  sink_radius;
+    double  sink_rate;
+    double  softening_length;      /* valid if has_softening_length         */
+    double  dt_min;                /* valid if has_dt_min                   */
+    int32_t has_plm_density_trigger;
+    int32_t one_body;
+    int32_t rk_order;              /* 1, 2 or 3                             */
+    int32_t has_mach_ceiling;
+    int32_t has_softening_length;
+    int32_t has_dt_min;
+} b2d_config;
+
+/*
+ * Where and why a step failed: HydroError (src/physics.rs:47-71) carries the
+ * error type and value, the zone position and the binary position.
+ */
+typedef struct b2d_error {
+    int32_t code;          /* b2d_status                                    */
+    int32_t run;           /* run index within a batch                      */
+    int32_t block_i, block_j, zone_i, zone_j;
+    double  value;         /* offending Σ or p                              */
+    double  x, y;          /* zone centre                                   */
+    double  time;          /* stage time at which it failed                 */
+    double  binary[4];     /* x1, y1, x2, y2 of the binary at that time     */
+} b2d_error;
+
+typedef struct b2d_ctx b2d_ctx;
+
+/* ------------------------------------------------------------------------ */
+/* Context life cycle. */
+
+/* Create a context for `nruns` runs (nruns = 1 for the reference's single
+ * run).  `cfgs` points to nruns configurations; runs may differ in mesh size
+ * and physics but share hydro kind, rk_order and precision.  Replaces the
+ * set-up of main.rs:run (tokio runtime, BlockData table; src/main.rs:114-122). */
+b2d_ctx* b2d_create(const b2d_config* cfgs, int32_t nruns, int32_t precision,
+                    b2d_status* status);
+void     b2d_destroy(b2d_ctx* ctx);
+
+/* Message of the last error raised on this thread (static storage). */
+const char* b2d_last_error(void);
+
+/* Number of conserved fields (3 or 4) of a context. */
+int32_t b2d_num_fields(const b2d_ctx* ctx);
+
+/* ------------------------------------------------------------------------ */
+/* State transfer.  Replaces moving a State into / out of scheme::advance
+ * (src/scheme.rs:323-331, state.rs:57-62) and building BlockData's
+ * initial_conserved background (scheme.rs:46-57). */
+
+/* Upload one run's conserved state and background (both in block layout),
+ * its time and iteration (Rational64 as numerator / denominator).  Resets that
+ * run's source ledger to zero unless `ledger` is non-NULL. */
+b2d_status b2d_upload_state(b2d_ctx* ctx, int32_t run, const double* cons,
+                            const double* background, const double* ledger,
+                            double time, int64_t iteration_num,
+                            int64_t iteration_den);
+
+/* Upload only the conserved state of one run (background and ledger kept). */
+b2d_status b2d_upload_conserved(b2d_ctx* ctx, int32_t run, const double* cons);
+
+/* Download one run's conserved state (block layout), time and iteration.
+ * Any output pointer may be NULL. */
+b2d_status b2d_download_state(b2d_ctx* ctx, int32_t run, double* cons,
+                              double* time, int64_t* iteration_num,
+                              int64_t* iteration_den);
+
+/* Download one run's per-block integrated source terms
+ * (BlockState::integrated_source_terms, src/state.rs:44-49). */
+b2d_status b2d_download_ledger(b2d_ctx* ctx, int32_t run, double* ledger);
+
+/* ------------------------------------------------------------------------ */
+/* The step.  scheme::advance (src/scheme.rs:323-349): dt = cfl·dx / max
+ * signal speed (floored by dt_min), then `fold` RK steps of
+ * try_advance_rk (scheme.rs:88-173) with the RK averaging of
+ * state.rs:183-252.  All runs of the context advance together, each with its
+ * own dt.  `dt_out` (nruns doubles) may be NULL; `err_out` may be NULL.
+ * On a hydro error the context's state is left as it was before the call,
+ * like the caller's copy of State in main.rs:159-205. */
+b2d_status b2d_advance(b2d_ctx* ctx, int32_t fold, double* dt_out,
+                       b2d_error* err_out);
+
+/* Enqueue an advance on the context's stream without waiting for it and
+ * without reading back dt or errors (for timing loops and graphs); a later
+ * b2d_synchronize() reports any error. */
+b2d_status b2d_advance_async(b2d_ctx* ctx, int32_t fold);
+b2d_status b2d_synchronize(b2d_ctx* ctx, double* dt_out, b2d_error* err_out);
+
+/* State::max_signal_speed (src/state.rs:121-133) of one run. */
+b2d_status b2d_max_signal_speed(b2d_ctx* ctx, int32_t run, double* out);
+
+/* ------------------------------------------------------------------------ */
+/* Initial conditions.  BlockState::from_model (src/state.rs:74-86) for the
+ * InfiniteDisk model (src/disks.rs:137-157), extended by a synthetic cavity
+ * and seeded multiplicative noise (both new: the reference has neither):
+ *   Σ = surface_density · max(cavity_floor, exp(-(cavity_radius / r)^12))
+ *       · (1 + noise · (2u - 1)),  u ~ U[0,1) from a counter hash of
+ *   (seed, run, global zone i, global zone j).
+ * cavity_radius = 0 disables the cavity; noise = 0 disables the noise.  The
+ * result is written in block layout.  Runs on the host. */
+typedef struct b2d_disk_model {
+    double   surface_density;
+    double   mach_number;      /* model Mach number (Euler); isothermal uses the hydro's */
+    double   cavity_radius;
+    double   cavity_floor;
+    double   noise;
+    uint64_t seed;
+    int32_t  run;
+    int32_t  pad_;
+} b2d_disk_model;
+
+b2d_status b2d_initial_state(const b2d_config* cfg, const b2d_disk_model* model,
+                             double* cons);
+
+/* ------------------------------------------------------------------------ */
+/* Tuning / introspection. */
+
+/* Tile shape of the stage kernel for a context: width in zones along j (a
+ * multiple of 32 dividing block_size) and height along i (dividing
+ * block_size).  0 keeps the current value. */
+b2d_status b2d_set_tile(b2d_ctx* ctx, int32_t tile_w, int32_t tile_h);
+b2d_status b2d_get_tile(const b2d_ctx* ctx, int32_t* tile_w, int32_t* tile_h);
+
+/* Use (1) or bypass (0) CUDA-graph replay of advance. Default 1. */
+b2d_status b2d_set_graphs(b2d_ctx* ctx, int32_t enable);
+
+/* Kernel launches issued by this context since creation. */
+int64_t b2d_launch_count(const b2d_ctx* ctx);
+
+/* Launches per advance of `fold` steps (for reporting). */
+int64_t b2d_launches_per_advance(const b2d_ctx* ctx, int32_t fold);
+
+/* Average device time of the stage kernel in the last timed window (ms), as
+ * measured with CUDA events on the context's stream; see b2d_time_stages. */
+b2d_status b2d_time_stages(b2d_ctx* ctx, int32_t fold, int32_t reps,
+                           double* ms_per_stage);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* B2D_H */
