@@ -213,6 +213,11 @@ class Runtime:
         return s.value or 0
 
 
+def set_device(device: int):
+    """Select the CUDA device of the calling thread inside libb2d."""
+    _check(_lib.load().b2d_set_device(int(device)))
+
+
 def pin(array: np.ndarray):
     """Page-lock a host array for asynchronous copies (cudaHostRegister)."""
     _check(_lib.load().b2d_pin_host(array.ctypes.data, array.nbytes))

@@ -80,10 +80,17 @@ __device__ void kepler_orbit(const RunDev& rd, double t, double* o)
 // (floored by dt_min, scheme.rs:336-340), the stage times of all `fold` RK
 // steps (try_advance_rk stamps t + dt, scheme.rs:168-170; weighted_average
 // averages time, state.rs:213-214), and the binary at each stage time.
-__global__ void prologue_kernel(const RunDev* runs, int fold, int rk, int start, int final_slot)
+__global__ void prologue_kernel(const RunDev* runs, int fold, int rk, int start, int final_slot,
+                                const unsigned long long* err_key, long long* adv_count)
 {
     const RunDev& rd = runs[blockIdx.x];
     const int stages = rk;
+    __shared__ int failed;
+    // a failure is pending: this advance and every later one are abandoned
+    if (threadIdx.x == 0) failed = (*(volatile const unsigned long long*)err_key != ~0ull);
+    __syncthreads();
+    if (failed) return;
+    if (threadIdx.x == 0 && blockIdx.x == 0) *adv_count += 1;
     if (threadIdx.x == 0) {
         double amax = __longlong_as_double((long long)*rd.amax);
         double dt = rd.p.cfl * rd.p.dx / amax;
@@ -209,6 +216,7 @@ struct RunHost {
     float *xcf = nullptr, *xvf = nullptr;
     double* stage_time = nullptr;
     double* orbit = nullptr;
+    std::vector<double> hxc;
 };
 
 // Host mirror of the per-context control block in device memory.
@@ -236,7 +244,11 @@ struct b2d_ctx {
     double* d_time = nullptr;         // [nruns][NSLOTS]
     long long* d_iter = nullptr;      // [nruns][NSLOTS]
     unsigned long long* d_amax = nullptr;  // [nruns]
-    b2d_error* d_err = nullptr;
+    unsigned long long* d_err_key = nullptr;  // failure key (~0: none)
+    unsigned* d_timeout = nullptr;            // a bounded wait gave up
+    long long* d_adv_count = nullptr;       // advances begun without a pending failure
+    long long adv_base = 0;
+    std::vector<std::pair<int, std::vector<StagePlan>>> window;  // advances since the last check
     double* d_staging = nullptr;
     size_t staging_bytes = 0;
     int max_stages = 0;
@@ -264,9 +276,9 @@ static size_t stage_smem_bytes(int nf, int rsize, int tw)
     return std::max(bytes, red);
 }
 
-static DevParams make_params(const b2d_config& c)
+template <class T> static DevParamsT<T> make_params(const b2d_config& c)
 {
-    DevParams p;
+    DevParamsT<T> p;
     memset(&p, 0, sizeof p);
     p.hydro = c.hydro_kind;
     p.visc = c.viscosity_kind;
@@ -280,37 +292,49 @@ static DevParams make_params(const b2d_config& c)
     p.cooling_slow_start = c.cooling_slow_start;
     p.has_dt_min = c.has_dt_min;
     double block_length = 2.0 * c.domain_radius / (double)c.num_blocks;  // mesh.rs:27-29
-    p.dx = block_length / (double)c.block_size;                          // mesh.rs:86-88
-    p.inv_dx = 1.0 / p.dx;
-    p.cfl = c.cfl;
-    p.dt_min = c.dt_min;
-    p.plm = c.plm;
-    p.pdt = c.has_plm_density_trigger ? c.plm_density_trigger : 0.0;     // scheme.rs:216-220
-    p.nu = c.viscosity;
-    p.lambda = c.lambda_multiplier;
-    p.mach2 = c.mach_number * c.mach_number;
-    p.gamma = c.hydro_kind == B2D_EULER ? c.gamma_law_index : 1.0;        // physics.rs:477-479
-    p.gm1 = p.gamma - 1.0;
-    p.sqrt_gm = sqrt(p.gamma);
+    double dx = block_length / (double)c.block_size;                     // mesh.rs:86-88
+    p.dx = (T)dx;
+    p.inv_dx = (T)(1.0 / dx);
+    p.cfl = (T)c.cfl;
+    p.dt_min = (T)c.dt_min;
+    p.plm = (T)c.plm;
+    p.pdt = (T)(c.has_plm_density_trigger ? c.plm_density_trigger : 0.0);  // scheme.rs:216-220
+    p.nu = (T)c.viscosity;
+    p.lambda = (T)c.lambda_multiplier;
+    p.mach2 = (T)(c.mach_number * c.mach_number);
+    p.inv_mach2 = (T)(1.0 / (c.mach_number * c.mach_number));
+    double gamma = c.hydro_kind == B2D_EULER ? c.gamma_law_index : 1.0;  // physics.rs:477-479
+    p.gamma = (T)gamma;
+    p.gm1 = (T)(gamma - 1.0);
+    p.inv_gm1 = (T)(1.0 / (gamma - 1.0));
+    p.sqrt_gm = (T)sqrt(gamma);
+    p.inv_sqrt_gm = (T)(1.0 / sqrt(gamma));
     double s = c.has_softening_length ? c.softening_length : c.sink_radius;  // physics.rs:399-405
-    p.soft2 = s * s;
-    p.sink_r2 = c.sink_radius * c.sink_radius;
-    p.sink_rate = c.sink_rate;
-    p.domain_radius = c.domain_radius;
-    p.buffer_scale = c.buffer_scale;
-    p.half_buffer_rate = 0.5 * c.buffer_rate;
+    p.soft2 = (T)(s * s);
+    p.sink_r2 = (T)(c.sink_radius * c.sink_radius);
+    p.inv_sink_r2 = (T)(1.0 / (c.sink_radius * c.sink_radius));
+    p.sink_rate = (T)c.sink_rate;
+    p.domain_radius = (T)c.domain_radius;
+    p.buffer_scale = (T)c.buffer_scale;
+    p.inv_buffer_scale = (T)(1.0 / c.buffer_scale);
+    p.half_buffer_rate = (T)(0.5 * c.buffer_rate);
     double q = c.one_body ? 1.0 : c.binary_mass_ratio;
     double m1 = 1.0 / (1.0 + q), m2 = 1.0 * q / (1.0 + q);
     double R = c.domain_radius;
-    p.omega_outer = sqrt((m1 + m2) / (R * R * R));                        // physics.rs:445
-    p.fake_thr = c.fake_mass_threshold;
-    p.fake_rate = c.fake_mass_rate;
-    p.density_floor = c.density_floor;
-    p.pressure_floor = c.pressure_floor;
-    p.density_floor_pow_gamma = c.has_density_floor ? pow(c.density_floor, p.gamma) : 0.0;
-    p.mach_ceiling2 = c.mach_ceiling * c.mach_ceiling;
-    p.cool_coef = c.cooling_coefficient;
-    p.cool_beta = c.cooling_beta;
+    double omega_outer = sqrt((m1 + m2) / (R * R * R));                  // physics.rs:445
+    p.omega_outer = (T)omega_outer;
+    p.half_rate_omega = (T)(0.5 * c.buffer_rate * omega_outer);
+    p.fake_thr = (T)c.fake_mass_threshold;
+    p.fake_rate = (T)c.fake_mass_rate;
+    p.density_floor = (T)c.density_floor;
+    p.pressure_floor = (T)c.pressure_floor;
+    p.density_floor_pow_gamma = (T)(c.has_density_floor ? pow(c.density_floor, gamma) : 0.0);
+    p.mach_ceiling2 = (T)(c.mach_ceiling * c.mach_ceiling);
+    p.k_mach_ceiling = (T)(c.has_mach_ceiling ? 2.0 / (gamma * (gamma - 1.0) * c.mach_ceiling * c.mach_ceiling) : 0.0);
+    p.cool_coef = (T)c.cooling_coefficient;
+    p.cool_beta = (T)c.cooling_beta;
+    p.inv_cool_beta = (T)(c.cooling_beta != 0.0 ? 1.0 / c.cooling_beta : 0.0);
+    p.eps_dx = (T)(1e-12 * dx);
     return p;
 }
 
@@ -323,6 +347,8 @@ static b2d_status validate(const b2d_config& c, int hydro, int rk)
     long long N = (long long)c.num_blocks * c.block_size;
     if (N * N > (1ll << 31)) return fail(B2D_ERR_INVALID, "mesh too large (more than 2^31 zones per run)");
     if (!(c.domain_radius > 0)) return fail(B2D_ERR_INVALID, "domain_radius must be positive");
+    if (c.num_blocks > 256 || c.block_size > 4096)
+        return fail(B2D_ERR_INVALID, "num_blocks must be at most 256 and block_size at most 4096");
     return B2D_OK;
 }
 
@@ -357,7 +383,7 @@ static void free_ctx(b2d_ctx* ctx)
         cudaFree(r.stage_time); cudaFree(r.orbit);
     }
     cudaFree(ctx->rdev); cudaFree(ctx->d_dt); cudaFree(ctx->d_time); cudaFree(ctx->d_iter);
-    cudaFree(ctx->d_amax); cudaFree(ctx->d_err); cudaFree(ctx->d_staging);
+    cudaFree(ctx->d_amax); cudaFree(ctx->d_err_key); cudaFree(ctx->d_adv_count); cudaFree(ctx->d_timeout); cudaFree(ctx->d_staging);
     for (cudaEvent_t e : ctx->ev) cudaEventDestroy(e);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -416,7 +442,7 @@ extern "C" b2d_ctx* b2d_create(const b2d_config* cfgs, int32_t nruns, int32_t pr
 {
     b2d_status st_dummy;
     if (!status) status = &st_dummy;
-    if (!cfgs || nruns < 1) { *status = fail(B2D_ERR_INVALID, "need at least one run"); return nullptr; }
+    if (!cfgs || nruns < 1 || nruns > 256) { *status = fail(B2D_ERR_INVALID, "need 1 to 256 runs"); return nullptr; }
     if (precision < 0 || precision > 2) { *status = fail(B2D_ERR_INVALID, "bad precision"); return nullptr; }
     int ndev = 0;
     cudaError_t ce = cudaGetDeviceCount(&ndev);
@@ -452,11 +478,15 @@ extern "C" b2d_ctx* b2d_create(const b2d_config* cfgs, int32_t nruns, int32_t pr
     CREATE_TRY(cudaMalloc(&ctx->d_time, sizeof(double) * nruns * NSLOTS));
     CREATE_TRY(cudaMalloc(&ctx->d_iter, sizeof(long long) * nruns * NSLOTS));
     CREATE_TRY(cudaMalloc(&ctx->d_amax, sizeof(unsigned long long) * nruns));
-    CREATE_TRY(cudaMalloc(&ctx->d_err, sizeof(b2d_error)));
+    CREATE_TRY(cudaMalloc(&ctx->d_err_key, sizeof(unsigned long long)));
+    CREATE_TRY(cudaMalloc(&ctx->d_adv_count, sizeof(long long)));
+    CREATE_TRY(cudaMalloc(&ctx->d_timeout, sizeof(unsigned)));
+    CREATE_TRY(cudaMemset(ctx->d_timeout, 0, sizeof(unsigned)));
+    CREATE_TRY(cudaMemset(ctx->d_adv_count, 0, sizeof(long long)));
     CREATE_TRY(cudaMemset(ctx->d_time, 0, sizeof(double) * nruns * NSLOTS));
     CREATE_TRY(cudaMemset(ctx->d_iter, 0, sizeof(long long) * nruns * NSLOTS));
     CREATE_TRY(cudaMemset(ctx->d_amax, 0, sizeof(unsigned long long) * nruns));
-    CREATE_TRY(cudaMemset(ctx->d_err, 0, sizeof(b2d_error)));
+    CREATE_TRY(cudaMemset(ctx->d_err_key, 0xff, sizeof(unsigned long long)));
     CREATE_TRY(cudaMemset(ctx->d_dt, 0, sizeof(double) * nruns));
 
     ctx->runs.resize(nruns);
@@ -491,6 +521,7 @@ extern "C" b2d_ctx* b2d_create(const b2d_config* cfgs, int32_t nruns, int32_t pr
             host_block_vertices(&cfgs[i], b, xv.data() + (size_t)b * (r.bs + 1));
         }
         std::vector<float> xcf(xc.begin(), xc.end()), xvf(xv.begin(), xv.end());
+        r.hxc = xc;
         CREATE_TRY(cudaMalloc(&r.xc, sizeof(double) * xc.size()));
         CREATE_TRY(cudaMalloc(&r.xv, sizeof(double) * xv.size()));
         CREATE_TRY(cudaMalloc(&r.xcf, sizeof(float) * xc.size()));
@@ -511,7 +542,8 @@ extern "C" b2d_ctx* b2d_create(const b2d_config* cfgs, int32_t nruns, int32_t pr
         d.amax = ctx->d_amax + i;
         d.binary_q = cfgs[i].binary_mass_ratio;
         d.binary_e = cfgs[i].binary_eccentricity;
-        d.p = make_params(cfgs[i]);
+        d.p = make_params<double>(cfgs[i]);
+        d.pf = make_params<float>(cfgs[i]);
         ctx->staging_bytes = std::max(ctx->staging_bytes, nn * ctx->nf * sizeof(double));
     }
     CREATE_TRY(cudaMalloc(&ctx->d_staging, ctx->staging_bytes));
@@ -708,7 +740,8 @@ static b2d_status launch_stage(b2d_ctx* ctx, const StagePlan& sp, int stage, int
     a.bf = sp.bf;
     a.w1f = split_df(-sp.bf + 1.0);
     a.bff = split_df(sp.bf);
-    a.err = ctx->d_err;
+    a.err_key = ctx->d_err_key;
+    a.timeout_flag = ctx->d_timeout;
     size_t smem = stage_smem_bytes(ctx->nf, rsize_of(ctx->precision), ctx->tw);
     cudaError_t e;
     if (ctx->precision == B2D_PREC_FP64) e = launch_stage_f64(ctx->nf, a, ctx->total_tiles, ctx->tw, smem, ctx->stream);
@@ -720,7 +753,8 @@ static b2d_status launch_stage(b2d_ctx* ctx, const StagePlan& sp, int stage, int
 static b2d_status enqueue_advance(b2d_ctx* ctx, int fold, int start, int* final_slot, bool count)
 {
     std::vector<StagePlan> plan = plan_advance(ctx->rk, fold, start, final_slot);
-    prologue_kernel<<<ctx->nruns, 32, 0, ctx->stream>>>(ctx->rdev, fold, ctx->rk, start, *final_slot);
+    prologue_kernel<<<ctx->nruns, 32, 0, ctx->stream>>>(ctx->rdev, fold, ctx->rk, start, *final_slot, ctx->d_err_key,
+                                                         ctx->d_adv_count);
     CUDA_TRY(cudaGetLastError());
     if (count) ctx->launches++;
     for (size_t s = 0; s < plan.size(); ++s) {
@@ -743,9 +777,14 @@ static b2d_status enqueue_advance(b2d_ctx* ctx, int fold, int start, int* final_
 
 static b2d_status run_advance(b2d_ctx* ctx, int fold, int* final_slot)
 {
+    if (fold * ctx->rk > 1023) return fail(B2D_ERR_INVALID, "fold x rk_order must be at most 1023");
     b2d_status st = ensure_stage_capacity(ctx, fold);
     if (st != B2D_OK) return st;
     const int start = ctx->cur;
+    {
+        int fs;
+        ctx->window.emplace_back(start, plan_advance(ctx->rk, fold, start, &fs));
+    }
     if (!ctx->use_graphs || ctx->instrument) {
         st = enqueue_advance(ctx, fold, start, final_slot, true);
         if (st != B2D_OK) return st;
@@ -781,37 +820,114 @@ static b2d_status run_advance(b2d_ctx* ctx, int fold, int* final_slot)
     return B2D_OK;
 }
 
-static b2d_status finish_advance(b2d_ctx* ctx, int start, int final_slot, double* dt_out, b2d_error* err_out)
+// Host restatement of try_to_primitive's failure value (physics.rs:489-503,
+// 631-660) for the zone named by a failure key.
+static double failure_value(const b2d_config& c, const double* u, int code)
 {
-    b2d_error err;
-    CUDA_TRY(cudaMemcpyAsync(&err, ctx->d_err, sizeof err, cudaMemcpyDeviceToHost, ctx->stream));
+    if (c.hydro_kind == B2D_ISOTHERMAL) return u[0];
+    double g = c.gamma_law_index;
+    double p[4] = {u[0], u[1] / u[0], u[2] / u[0], 0.0};
+    p[3] = (u[3] - 0.5 * u[0] * (p[1] * p[1] + p[2] * p[2])) * (g - 1.0);
+    if (c.has_density_floor && p[0] < c.density_floor) {
+        p[0] = c.density_floor; p[1] = 0.0; p[2] = 0.0; p[3] = pow(c.density_floor, g);
+    }
+    if (code == 1) return p[0];
+    if (c.has_pressure_floor && p[3] < c.pressure_floor) p[3] = c.pressure_floor;
+    return p[3];
+}
+
+static b2d_status decode_failure(b2d_ctx* ctx, unsigned long long key, const std::vector<StagePlan>& plan,
+                                 b2d_error* e)
+{
+    memset(e, 0, sizeof *e);
+    const int stage = (int)(key >> 54);
+    const int run = (int)((key >> 46) & 0xff);
+    const int blk = (int)((key >> 30) & 0xffff);
+    const int order = (int)((key >> 26) & 0xf);
+    const int zone = (int)((key >> 2) & 0xffffff);
+    e->code = (int)(key & 3);
+    e->run = run;
+    RunHost& r = ctx->runs[run];
+    const int nb = r.nb, bs = r.bs;
+    const int bi = blk / nb, bj = blk % nb, di = order / 3 - 1, dj = order % 3 - 1;
+    e->block_i = (bi + di + nb) % nb;
+    e->block_j = (bj + dj + nb) % nb;
+    e->zone_i = zone / bs;
+    e->zone_j = zone % bs;
+    const int gi = e->block_i * bs + e->zone_i, gj = e->block_j * bs + e->zone_j;
+    e->x = r.hxc[gi];
+    e->y = r.hxc[gj];
+    const size_t nn = (size_t)r.N * r.N, idx = (size_t)gi * r.N + gj;
+    const int slot = plan.at(stage).in;
+    double u[4] = {0, 0, 0, 0};
+    for (int f = 0; f < ctx->nf; ++f) {
+        if (store_of(ctx) == 0) {
+            CUDA_TRY(cudaMemcpy(&u[f], (const double*)r.slot[slot] + f * nn + idx, sizeof(double), cudaMemcpyDeviceToHost));
+        } else {
+            float hl[2];
+            CUDA_TRY(cudaMemcpy(&hl[0], (const float*)r.slot[slot] + (2 * f) * nn + idx, sizeof(float), cudaMemcpyDeviceToHost));
+            CUDA_TRY(cudaMemcpy(&hl[1], (const float*)r.slot[slot] + (2 * f + 1) * nn + idx, sizeof(float), cudaMemcpyDeviceToHost));
+            u[f] = (double)hl[0] + (double)hl[1];
+        }
+    }
+    e->value = failure_value(r.cfg, u, e->code);
+    double orb[10];
+    CUDA_TRY(cudaMemcpy(&e->time, r.stage_time + stage, sizeof(double), cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(orb, r.orbit + 10 * stage, sizeof orb, cudaMemcpyDeviceToHost));
+    e->binary[0] = orb[1]; e->binary[1] = orb[2]; e->binary[2] = orb[6]; e->binary[3] = orb[7];
+    return B2D_OK;
+}
+
+static b2d_status finish_advance(b2d_ctx* ctx, int final_slot, double* dt_out, b2d_error* err_out)
+{
+    unsigned long long key = ~0ull;
+    long long count = 0;
+    CUDA_TRY(cudaMemcpyAsync(&key, ctx->d_err_key, sizeof key, cudaMemcpyDeviceToHost, ctx->stream));
+    CUDA_TRY(cudaMemcpyAsync(&count, ctx->d_adv_count, sizeof count, cudaMemcpyDeviceToHost, ctx->stream));
+    unsigned tmo = 0;
+    CUDA_TRY(cudaMemcpyAsync(&tmo, ctx->d_timeout, sizeof tmo, cudaMemcpyDeviceToHost, ctx->stream));
     std::vector<double> dts(ctx->nruns);
     CUDA_TRY(cudaMemcpyAsync(dts.data(), ctx->d_dt, sizeof(double) * ctx->nruns, cudaMemcpyDeviceToHost, ctx->stream));
     CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    auto window = std::move(ctx->window);
+    ctx->window.clear();
+    const long long base = ctx->adv_base;
+    ctx->adv_base = count;
     if (dt_out) memcpy(dt_out, dts.data(), sizeof(double) * ctx->nruns);
-    if (err.code != 0) {
+    if (tmo) {
+        CUDA_TRY(cudaMemsetAsync(ctx->d_timeout, 0, sizeof(unsigned), ctx->stream));
+        CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+        return fail(B2D_ERR_TIMEOUT, "a bounded wait on a staging barrier gave up; the step's results are invalid");
+    }
+    if (key != ~0ull) {
+        // the failing advance is the last one whose prologue ran
+        long long k = count - 1 - base;
+        if (k < 0 || k >= (long long)window.size()) return fail(B2D_ERR_CUDA, "failure bookkeeping lost");
+        const int start = window[k].first;
+        b2d_error err;
+        b2d_status s = decode_failure(ctx, key, window[k].second, &err);
+        if (s != B2D_OK) return s;
         if (err_out) *err_out = err;
-        CUDA_TRY(cudaMemsetAsync(ctx->d_err, 0, sizeof(b2d_error), ctx->stream));
+        CUDA_TRY(cudaMemsetAsync(ctx->d_err_key, 0xff, sizeof(unsigned long long), ctx->stream));
         ctx->cur = start;
         for (int r = 0; r < ctx->nruns; ++r) {
-            b2d_status s = launch_max_speed(ctx, r, start);
+            s = launch_max_speed(ctx, r, start);
             if (s != B2D_OK) return s;
         }
         CUDA_TRY(cudaStreamSynchronize(ctx->stream));
         return fail((b2d_status)err.code, "hydro error during advance");
     }
-    ctx->cur = final_slot;
+    if (final_slot >= 0) ctx->cur = final_slot;
     return B2D_OK;
 }
 
 extern "C" b2d_status b2d_advance(b2d_ctx* ctx, int32_t fold, double* dt_out, b2d_error* err_out)
 {
     if (!ctx || fold < 1) return fail(B2D_ERR_INVALID, "bad arguments");
-    const int start = ctx->cur;
     int final_slot = -1;
     b2d_status st = run_advance(ctx, fold, &final_slot);
     if (st != B2D_OK) return st;
-    return finish_advance(ctx, start, final_slot, dt_out, err_out);
+    return finish_advance(ctx, final_slot, dt_out, err_out);
 }
 
 extern "C" b2d_status b2d_advance_async(b2d_ctx* ctx, int32_t fold)
@@ -827,7 +943,7 @@ extern "C" b2d_status b2d_advance_async(b2d_ctx* ctx, int32_t fold)
 extern "C" b2d_status b2d_synchronize(b2d_ctx* ctx, double* dt_out, b2d_error* err_out)
 {
     if (!ctx) return fail(B2D_ERR_INVALID, "bad arguments");
-    return finish_advance(ctx, ctx->cur, ctx->cur, dt_out, err_out);
+    return finish_advance(ctx, -1, dt_out, err_out);
 }
 
 extern "C" b2d_status b2d_set_tile(b2d_ctx* ctx, int32_t tile_w, int32_t tile_h)
@@ -912,5 +1028,11 @@ extern "C" b2d_status b2d_pin_host(void* ptr, uint64_t bytes)
 extern "C" b2d_status b2d_unpin_host(void* ptr)
 {
     CUDA_TRY(cudaHostUnregister(ptr));
+    return B2D_OK;
+}
+
+extern "C" b2d_status b2d_set_device(int32_t device)
+{
+    CUDA_TRY(cudaSetDevice(device));
     return B2D_OK;
 }

@@ -1,11 +1,33 @@
 // kernels_f32.cu — FP32-stencil stage kernels over FP64 state (store 0) or
-// compensated FP32 state (store 1).
+// compensated FP32 state (store 1).  Tiles whose width is a multiple of 32
+// run the TMA-staged kernel of stage2.cuh; narrower tiles (blocks of fewer
+// than 32 zones) run the generic kernel of stage.cuh.
 #include "kernels.inc"
+#include "stage2.cuh"
 
 namespace b2d {
 
+template <int NF, int STORE>
+static cudaError_t launch_two(const StageArgs& a, int grid, int tw, cudaStream_t s)
+{
+    auto k = stage2_kernel<NF, STORE>;
+    size_t smem = s2_smem_bytes(NF, STORE, tw);
+    static size_t configured = 0;
+    if (smem > 48 * 1024 && smem > configured) {
+        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        configured = smem;
+    }
+    k<<<grid, tw + 32, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_stage_f32(int nf, int store, const StageArgs& a, int grid, int tw, size_t smem, cudaStream_t s)
 {
+    if (tw % 32 == 0 && tw <= 128) {
+        if (nf == 3) return store == 0 ? launch_two<3, 0>(a, grid, tw, s) : launch_two<3, 1>(a, grid, tw, s);
+        return store == 0 ? launch_two<4, 0>(a, grid, tw, s) : launch_two<4, 1>(a, grid, tw, s);
+    }
     if (nf == 3) {
         if (store == 0) return launch_one<3, float, 0>(a, grid, tw, smem, s);
         return launch_one<3, float, 1>(a, grid, tw, smem, s);

@@ -18,30 +18,36 @@ namespace b2d {
 
 enum { SINK1 = 0, SINK2, GRAV1, GRAV2, BUFFER, COOLING, FAKE_MASS, NITEMS };
 
-// Physics parameters in device form (built on the host from b2d_config).
-struct DevParams {
+// Physics parameters in device form, built on the host from b2d_config.
+// DevParamsT<double> serves the FP64 kernels, DevParamsT<float> the FP32
+// kernels (no double arithmetic or conversion in their inner loops).
+template <class T> struct DevParamsT {
     int hydro;            // 0 iso, 1 euler
     int visc;             // 0 constant nu, 1 alpha
     int sink_model;       // 0 impartial, 1 torque-free
     int one_body;
     int has_mach_ceiling, has_density_floor, has_pressure_floor, density_index;
     int cooling_kind, cooling_slow_start, has_dt_min, pad_;
-    double dx, inv_dx;
-    double cfl, dt_min;
-    double plm, pdt;                  // θ and the PLM density trigger (0 if unset)
-    double nu;                        // ν or α
-    double lambda;                    // lambda_multiplier
-    double mach2;                     // mach_number²  (iso)
-    double gamma, gm1;                // γ and γ - 1 (euler; iso γ = 1)
-    double sqrt_gm;                   // sqrt(γ) for α viscosity
-    double soft2;                     // softening_length²
-    double sink_r2, sink_rate;        // sink_radius², sink_rate
-    double domain_radius, buffer_scale, half_buffer_rate, omega_outer;
-    double fake_thr, fake_rate;
-    double density_floor, pressure_floor, density_floor_pow_gamma;
-    double mach_ceiling2;             // mach_ceiling²
-    double cool_coef, cool_beta;
+    T dx, inv_dx;
+    T cfl, dt_min;
+    T plm, pdt;                       // θ and the PLM density trigger (0 if unset)
+    T nu;                             // ν or α
+    T lambda;                         // lambda_multiplier
+    T mach2, inv_mach2;               // mach_number² (iso)
+    T gamma, gm1, inv_gm1;            // γ, γ - 1 (euler; iso γ = 1)
+    T sqrt_gm, inv_sqrt_gm;           // sqrt(γ) for α viscosity
+    T soft2;                          // softening_length²
+    T sink_r2, inv_sink_r2, sink_rate;
+    T domain_radius, buffer_scale, inv_buffer_scale, half_buffer_rate, omega_outer, half_rate_omega;
+    T fake_thr, fake_rate;
+    T density_floor, pressure_floor, density_floor_pow_gamma;
+    T mach_ceiling2;                  // mach_ceiling²
+    T k_mach_ceiling;                 // 2 / (γ (γ - 1) mach_ceiling²)
+    T cool_coef, cool_beta, inv_cool_beta;
+    T eps_dx;                         // 1e-12 · dx (α viscosity)
 };
+using DevParams = DevParamsT<double>;
+using DevParamsF = DevParamsT<float>;
 
 template <class R> struct PointMass { R m, x, y, vx, vy; };
 template <class R> struct Binary { PointMass<R> p1, p2; };
@@ -113,7 +119,7 @@ template <class R> __device__ __forceinline__ R binary_potential(const Binary<R>
 
 // ---------------------------------------------------------------------------
 // Conserved <-> primitive (hydro-iso2d / hydro-euler, restated).
-template <int NF, class R> __device__ __forceinline__ void prim_to_cons(const DevParams& P, const R* p, R* u)
+template <int NF, class R> __device__ __forceinline__ void prim_to_cons(const DevParamsT<R>& P, const R* p, R* u)
 {
     u[0] = p[0];
     u[1] = p[0] * p[1];
@@ -122,11 +128,11 @@ template <int NF, class R> __device__ __forceinline__ void prim_to_cons(const De
         if constexpr (std::is_same<R, double>::value)
             u[3] = 0.5 * p[0] * (p[1] * p[1] + p[2] * p[2]) + p[3] / P.gm1;
         else
-            u[3] = 0.5f * p[0] * (p[1] * p[1] + p[2] * p[2]) + p[3] * (float)(1.0 / P.gm1);
+            u[3] = 0.5f * p[0] * (p[1] * p[1] + p[2] * p[2]) + p[3] * P.inv_gm1;
     }
 }
 
-template <int NF, class R> __device__ __forceinline__ void cons_to_prim_raw(const DevParams& P, const R* u, R* p)
+template <int NF, class R> __device__ __forceinline__ void cons_to_prim_raw(const DevParamsT<R>& P, const R* u, R* p)
 {
     p[0] = u[0];
     if constexpr (std::is_same<R, double>::value) {
@@ -137,14 +143,14 @@ template <int NF, class R> __device__ __forceinline__ void cons_to_prim_raw(cons
         float ir = __frcp_rn(u[0]);
         p[1] = u[1] * ir;
         p[2] = u[2] * ir;
-        if constexpr (NF == 4) p[3] = (u[3] - 0.5f * u[0] * (p[1] * p[1] + p[2] * p[2])) * (float)P.gm1;
+        if constexpr (NF == 4) p[3] = (u[3] - 0.5f * u[0] * (p[1] * p[1] + p[2] * p[2])) * P.gm1;
     }
 }
 
 // Hydrodynamics::try_to_primitive (physics.rs:489-503 iso, 631-660 euler).
 // Returns 0, 1 (negative density) or 2 (negative pressure).
 template <int NF, class R>
-__device__ __forceinline__ int try_to_primitive(const DevParams& P, const R* u_in, R* p, R& bad)
+__device__ __forceinline__ int try_to_primitive(const DevParamsT<R>& P, const R* u_in, R* p, R& bad)
 {
     if constexpr (NF == 3) {
         R u[3] = {u_in[0], u_in[1], u_in[2]};
@@ -172,7 +178,7 @@ __device__ __forceinline__ int try_to_primitive(const DevParams& P, const R* u_i
 }
 
 // Hydrodynamics::max_signal_speed (physics.rs:521-526 iso; 679-681 euler).
-template <int NF, class R> __device__ __forceinline__ R max_signal_speed(const DevParams& P, const R* u)
+template <int NF, class R> __device__ __forceinline__ R max_signal_speed(const DevParamsT<R>& P, const R* u)
 {
     R p[NF];
     cons_to_prim_raw<NF, R>(P, u, p);
@@ -197,7 +203,7 @@ __device__ __forceinline__ void physical_flux(const R* p, const R* u, int axis, 
 }
 
 template <int NF, class R>
-__device__ __forceinline__ void hlle(const DevParams& P, const R* pl, const R* pr, int axis, R cs2, R* F)
+__device__ __forceinline__ void hlle(const DevParamsT<R>& P, const R* pl, const R* pr, int axis, R cs2, R* F)
 {
     R ul[NF], ur[NF], fl[NF], fr[NF];
     prim_to_cons<NF, R>(P, pl, ul);
@@ -242,7 +248,7 @@ template <int NF> struct CellLayout {
 };
 
 // Velocity-gradient terms of stress_field, evaluated once per cell.
-template <int NF, class R> __device__ __forceinline__ void cell_shear(const DevParams& P, R* rec)
+template <int NF, class R> __device__ __forceinline__ void cell_shear(const DevParamsT<R>& P, R* rec)
 {
     using L = CellLayout<NF>;
     const R gxvx = rec[L::GX + 1], gxvy = rec[L::GX + 2], gyvx = rec[L::GY + 1], gyvy = rec[L::GY + 2];
@@ -253,7 +259,7 @@ template <int NF, class R> __device__ __forceinline__ void cell_shear(const DevP
         rec[L::SYY] = -2.0 / 3.0 * gxvx / dx + 4.0 / 3.0 * gyvy / dy;
         rec[L::BULK] = gxvx / dx + gyvy / dy;
     } else {
-        const float id = (float)P.inv_dx;
+        const float id = P.inv_dx;
         const float a = gxvx * id, b = gyvy * id;
         rec[L::SXX] = (4.0f / 3.0f) * a - (2.0f / 3.0f) * b;
         rec[L::SXY] = (gxvy + gyvx) * id;
@@ -276,7 +282,7 @@ __device__ __forceinline__ R stress(const R* rec, R nu, R lam_nu, int row, int c
 
 // The `nu` closure of compute_block_fluxes (scheme.rs:230-247).
 template <int NF, class R>
-__device__ __forceinline__ R face_nu(const DevParams& P, const Binary<R>& b, R x, R y, const R* rec)
+__device__ __forceinline__ R face_nu(const DevParamsT<R>& P, const Binary<R>& b, R x, R y, const R* rec)
 {
     if (P.visc == 0) return R(P.nu);
     using L = CellLayout<NF>;
@@ -286,21 +292,22 @@ __device__ __forceinline__ R face_nu(const DevParams& P, const Binary<R>& b, R x
     R cs2;
     if constexpr (NF == 3) {
         R gpot = binary_potential(b, x, y, R(P.soft2));
-        cs2 = dvd(-gpot, R(P.mach2));
+        if constexpr (std::is_same<R, double>::value) cs2 = -gpot / P.mach2;
+        else cs2 = -gpot * P.inv_mach2;
     } else {
-        cs2 = R(P.gamma) * rec[L::PC + 3] / rec[L::PC];
+        cs2 = dvd(P.gamma * rec[L::PC + 3], rec[L::PC]);
     }
-    R eps = R(1e-12) * R(P.dx);
+    R eps = P.eps_dx;
     R a1 = r1 + eps, a2 = r2 + eps;
     R twofreq = rsqrt_(b.p1.m / (a1 * a1 * a1) + b.p2.m / (a2 * a2 * a2));
     if constexpr (std::is_same<R, double>::value) return P.nu * cs2 / twofreq / P.sqrt_gm;
-    else return dvd(dvd(float(P.nu) * cs2, twofreq), float(P.sqrt_gm));
+    else return dvd(P.nu * cs2, twofreq) * P.inv_sqrt_gm;
 }
 
 // Hydrodynamics::intercell_flux (physics.rs:584-607 iso, 776-803 euler) for
 // cells l, r across a face at (x, y) normal to `axis`.
 template <int NF, class R>
-__device__ __forceinline__ void intercell_flux(const DevParams& P, const Binary<R>& b, const R* l, const R* r, R x,
+__device__ __forceinline__ void intercell_flux(const DevParamsT<R>& P, const Binary<R>& b, const R* l, const R* r, R x,
                                                R y, int axis, R* F)
 {
     using L = CellLayout<NF>;
@@ -319,7 +326,8 @@ __device__ __forceinline__ void intercell_flux(const DevParams& P, const Binary<
     R cs2 = R(0);
     if constexpr (NF == 3) {
         R phi = binary_potential(b, x, y, R(P.soft2));
-        cs2 = dvd(-phi, R(P.mach2));
+        if constexpr (std::is_same<R, double>::value) cs2 = -phi / P.mach2;
+        else cs2 = -phi * P.inv_mach2;
     }
     hlle<NF, R>(P, pl, pr, axis, cs2, F);
     F[0] = F[0] + R(0);
@@ -336,19 +344,21 @@ __device__ __forceinline__ void intercell_flux(const DevParams& P, const Binary<
 // Source terms.  Physics::sink_kernel (physics.rs:388-397), Physics::source_terms
 // (physics.rs:423-457), Isothermal::source_terms (physics.rs:528-582),
 // Euler::source_terms (physics.rs:683-774).
-template <class R> __device__ __forceinline__ R sink_kernel(const DevParams& P, R dx, R dy)
+template <class R> __device__ __forceinline__ R sink_kernel(const DevParamsT<R>& P, R dx, R dy)
 {
     R r2 = dx * dx + dy * dy;
     R s2 = R(P.sink_r2);
     if (r2 < s2) {
-        R t = R(1) - dvd(r2, s2);
+        R t;
+        if constexpr (std::is_same<R, double>::value) t = 1.0 - r2 / s2;
+        else t = 1.0f - r2 * P.inv_sink_r2;
         return R(P.sink_rate) * (t * t);
     }
     return R(0);
 }
 
 template <class R>
-__device__ __forceinline__ void torque_free_velocity(const DevParams& P, const PointMass<R>& b, R x, R y, R vx, R vy,
+__device__ __forceinline__ void torque_free_velocity(const DevParamsT<R>& P, const PointMass<R>& b, R x, R y, R vx, R vy,
                                                      R& vxc, R& vyc)
 {
     R vxb = P.one_body ? R(0) : b.vx;
@@ -361,7 +371,7 @@ __device__ __forceinline__ void torque_free_velocity(const DevParams& P, const P
 }
 
 // Buffer rate 0.5·rate·(1 + tanh((r - R)/scale))·Ω_outer (physics.rs:443-446).
-template <class R> __device__ __forceinline__ R buffer_rate(const DevParams& P, R x, R y)
+template <class R> __device__ __forceinline__ R buffer_rate(const DevParamsT<R>& P, R x, R y)
 {
     if constexpr (std::is_same<R, double>::value) {
         double r = sqrt(x * x + y * y);
@@ -370,14 +380,14 @@ template <class R> __device__ __forceinline__ R buffer_rate(const DevParams& P, 
     } else {
         // 1 + tanh(y) = 2 / (1 + exp(-2y))
         float r = sqrtf(x * x + y * y);
-        float yb = (r - (float)P.domain_radius) * (float)(1.0 / P.buffer_scale);
+        float yb = (r - P.domain_radius) * P.inv_buffer_scale;
         float e = __expf(-2.0f * yb);
-        return (float)(P.half_buffer_rate * P.omega_outer) * __fdividef(2.0f, 1.0f + e);
+        return P.half_rate_omega * __fdividef(2.0f, 1.0f + e);
     }
 }
 
 template <int NF, class R>
-__device__ __forceinline__ void source_terms(const DevParams& P, const Binary<R>& b, const R* u, const R* u0, R x, R y,
+__device__ __forceinline__ void source_terms(const DevParamsT<R>& P, const Binary<R>& b, const R* u, const R* u0, R x, R y,
                                              R t, R dt, R* it /* [NITEMS][NF] */)
 {
     const R s2 = R(P.soft2);
@@ -438,7 +448,7 @@ __device__ __forceinline__ void source_terms(const DevParams& P, const Binary<R>
         const R g = R(P.gamma);
         R e0;
         if constexpr (std::is_same<R, double>::value) e0 = p0[3] / p0[0] / P.gm1;
-        else e0 = dvd(p0[3], p0[0]) * (float)(1.0 / P.gm1);
+        else e0 = dvd(p0[3], p0[0]) * P.inv_gm1;
         R ec;
         if (P.cooling_kind == 1) {
             // β-cooling (not in the reference): e → e·exp(-Ω dt / β)
@@ -452,7 +462,7 @@ __device__ __forceinline__ void source_terms(const DevParams& P, const Binary<R>
                 om = sqrtf(b.p1.m * q1 * q1 * q1 + b.p2.m * q2 * q2 * q2);
             }
             if constexpr (std::is_same<R, double>::value) ec = e0 * exp(-om * dt / P.cool_beta);
-            else ec = e0 * __expf(-om * dt * (float)(1.0 / P.cool_beta));
+            else ec = e0 * __expf(-om * dt * P.inv_cool_beta);
         } else {
             R f = R(1);
             if (P.cooling_slow_start) {
@@ -468,7 +478,7 @@ __device__ __forceinline__ void source_terms(const DevParams& P, const Binary<R>
         if (P.has_mach_ceiling) {
             R ek = R(0.5) * (p0[1] * p0[1] + p0[2] * p0[2]);
             if constexpr (std::is_same<R, double>::value) ec = fmax(ec, 2.0 * ek / g / P.gm1 / P.mach_ceiling2);
-            else ec = fmaxf(ec, 2.0f * ek * (float)(1.0 / (P.gamma * P.gm1 * P.mach_ceiling2)));
+            else ec = fmaxf(ec, ek * P.k_mach_ceiling);
         }
         R pc[4] = {p0[0], p0[1], p0[2], p0[0] * ec * R(P.gm1)};
         R uc[4];

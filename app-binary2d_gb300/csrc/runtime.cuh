@@ -31,7 +31,8 @@ struct RunDev {
     double* orbit;           // [max_stages][10]: m, x, y, vx, vy of body 1 then body 2
     unsigned long long* amax;
     double binary_q, binary_e;
-    DevParams p;
+    DevParams p;     // FP64 kernels
+    DevParamsF pf;   // FP32 kernels
 };
 
 struct StageArgs {
@@ -43,7 +44,12 @@ struct StageArgs {
     int amax_flag;
     double bf;               // weight of the RK base state (br of godunov-core)
     b2d::df32w w1f, bff;     // 1 - bf and bf as double-float
-    b2d_error* err;
+    unsigned long long* err_key;  // failure key, ~0 when no zone failed
+    unsigned* timeout_flag;       // set when a bounded wait gave up
 };
+
+template <class R> __host__ __device__ inline const DevParamsT<R>& params_of(const RunDev& rd);
+template <> __host__ __device__ inline const DevParamsT<double>& params_of<double>(const RunDev& rd) { return rd.p; }
+template <> __host__ __device__ inline const DevParamsT<float>& params_of<float>(const RunDev& rd) { return rd.pf; }
 
 }  // namespace b2d

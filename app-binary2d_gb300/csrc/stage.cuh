@@ -106,24 +106,29 @@ template <> struct State<1> {
 
 __device__ __forceinline__ int wrap(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
 
-__device__ __forceinline__ void report_error(b2d_error* err, int code, int run, const RunDev& rd, int gi, int gj,
-                                             double value, double x, double y, double time, const double* orb)
+// Failure key of a zone: the reference surfaces the error of the first
+// block, in mesh.block_indexes() order, whose 3x3 neighbour join fails
+// (scheme.rs:126, 161-165); within that block the first failing neighbour
+// in neighbour order (mesh.rs:101-110), within that neighbour the first
+// failing zone in row-major order (scheme.rs:190-197).  The smallest key
+// over all failing zones of the earliest failing stage is that error:
+//   stage:10 | run:8 | block:16 | neighbour order:4 | zone:24 | code:2
+__device__ __forceinline__ unsigned long long error_key(int stage, int run, const RunDev& rd, int gi, int gj, int code)
 {
-    if (atomicCAS(&err->code, 0, code) == 0) {
-        err->run = run;
-        err->block_i = gi / rd.bs;
-        err->block_j = gj / rd.bs;
-        err->zone_i = gi % rd.bs;
-        err->zone_j = gj % rd.bs;
-        err->value = value;
-        err->x = x;
-        err->y = y;
-        err->time = time;
-        err->binary[0] = orb[1];
-        err->binary[1] = orb[2];
-        err->binary[2] = orb[6];
-        err->binary[3] = orb[7];
-    }
+    const int nb = rd.nb, bs = rd.bs;
+    const int ni = gi / bs, nj = gj / bs;
+    const unsigned long long zone = (unsigned long long)((gi % bs) * bs + (gj % bs));
+    unsigned long long best = ~0ull;
+    for (int di = -1; di <= 1; ++di)
+        for (int dj = -1; dj <= 1; ++dj) {
+            int bi = (ni - di + nb) % nb, bj = (nj - dj + nb) % nb;   // n = b + (di, dj)
+            unsigned long long k = ((unsigned long long)stage << 54) | ((unsigned long long)run << 46) |
+                                   ((unsigned long long)(bi * nb + bj) << 30) |
+                                   ((unsigned long long)((di + 1) * 3 + (dj + 1)) << 26) | (zone << 2) |
+                                   (unsigned long long)code;
+            best = k < best ? k : best;
+        }
+    return best;
 }
 
 // ----------------------------------------------------------------------------
@@ -147,10 +152,15 @@ __global__ void __launch_bounds__(256) stage_kernel(StageArgs a)
     const RunDev& rd = a.runs[ri];
     if (g - rd.tile_base >= rd.ntiles) return;
 
-    __shared__ DevParams P;
+    __shared__ DevParamsT<R> P;
     __shared__ Binary<R> B;
     __shared__ double orbd[10];
-    if (t == 0) P = rd.p;
+    __shared__ int failed;
+    // an earlier stage failed: the advance is abandoned (the caller keeps its state)
+    if (t == 0) failed = (*(volatile unsigned long long*)a.err_key != ~0ull);
+    __syncthreads();
+    if (failed) return;
+    if (t == 0) P = params_of<R>(rd);
     if (t < 10) orbd[t] = rd.orbit[a.stage * 10 + t];
     __syncthreads();
     if (t == 0) {
@@ -207,9 +217,10 @@ __global__ void __launch_bounds__(256) stage_kernel(StageArgs a)
 #pragma unroll
                 for (int f = 0; f < NF; ++f) u[f] = S::template load_r<R>(uin, nn, idx, f);
                 R bad = R(0);
+                (void)bad;
                 int e = try_to_primitive<NF, R>(P, u, p, bad);
                 if (e && rn >= 0 && rn < TH && c >= 0 && c < TW)
-                    report_error(a.err, e, ri, rd, gi, gj, (double)bad, rd.xc[gi], rd.xc[gj], timed, orbd);
+                    atomicMin(a.err_key, error_key(a.stage, ri, rd, gi, gj, e));
 #pragma unroll
                 for (int f = 0; f < NF; ++f) row[(c + 2) * NF + f] = p[f];
             }
@@ -340,7 +351,7 @@ __global__ void __launch_bounds__(256) stage_kernel(StageArgs a)
 
     // --- per-tile ledger and max speed -----------------------------------------
     double* red = (double*)smem_raw;  // [TW] scratch, reused after the loop
-    const double area = P.dx * P.dx;
+    const double area = rd.p.dx * rd.p.dx;
     for (int k = 0; k < NL; ++k) {
         red[t] = (double)led[k];
         __syncthreads();

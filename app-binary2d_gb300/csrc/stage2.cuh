@@ -1,0 +1,466 @@
+// stage2.cuh — the FP32-stencil RK-stage kernel with TMA row staging.
+//
+// Same stage as stage.cuh (try_advance_rk, src/scheme.rs:88-173, plus the RK
+// average of state.rs:183-199), reorganised for throughput:
+//
+//  * Row staging by TMA.  One producer lane issues 1-D bulk copies
+//    (cp.async.bulk) of whole tile rows — the stage input with its 2-zone
+//    guard halo (wrapped periodically, mesh.rs:101-110), the background and
+//    the RK base — into a ring of shared-memory slots, DEPTH rows ahead of
+//    use.  Each slot completes on its own mbarrier; every wait is bounded.
+//  * Column ownership.  Thread t < TW owns column t of the tile and keeps
+//    that column's vertical history (primitives, cell records, x-fluxes) in
+//    registers.  A fifth "halo" warp owns the four guard columns.  Shared
+//    memory only carries the horizontal exchange (primitives for the y slope,
+//    cell records for the y face, y fluxes for the right face), in float4
+//    planes that are free of bank conflicts.
+//  * Pipeline per marching row rn: load/convert row rn, slopes and cell
+//    records of row rn-1, fluxes of row rn-2, update of row rn-3; one
+//    __syncthreads per row.
+#pragma once
+
+#include "stage.cuh"
+#include "tma.cuh"
+
+namespace b2d {
+
+constexpr int S2_DEPTH = 2;              // rows staged ahead of use
+constexpr int S2_SLOTS = S2_DEPTH + 4;   // a slot is read up to 3 rows after it lands
+
+// Bytes of one staging slot (one tile row).
+__host__ __device__ inline int s2_slot_bytes(int nf, int store, int tw)
+{
+    if (store == 1) return 4 * (nf * (tw + 8) + 4 * nf * tw);   // hi (+halo) | lo | bg hi | base hi | base lo
+    return 8 * (nf * (tw + 4) + 2 * nf * tw);                   // state (+halo) | bg | base
+}
+
+__host__ __device__ inline int s2_smem_bytes(int nf, int store, int tw)
+{
+    int slots = S2_SLOTS * s2_slot_bytes(nf, store, tw);
+    int exch = 16 * (2 * (tw + 4) + 3 * 2 * (tw + 2) + 2 * (tw + 1));
+    return slots + exch + 8 * S2_SLOTS;
+}
+
+template <int NF>
+__device__ __forceinline__ float alpha_nu_f(const DevParamsF& P, const Binary<float>& b, float x, float y,
+                                            const float* pc)
+{
+    float dx1 = x - b.p1.x, dy1 = y - b.p1.y, dx2 = x - b.p2.x, dy2 = y - b.p2.y;
+    float a1 = sqrtf(dx1 * dx1 + dy1 * dy1) + P.eps_dx;
+    float a2 = sqrtf(dx2 * dx2 + dy2 * dy2) + P.eps_dx;
+    float cs2;
+    if constexpr (NF == 3) cs2 = -binary_potential(b, x, y, P.soft2) * P.inv_mach2;
+    else cs2 = __fdividef(P.gamma * pc[3], pc[0]);
+    float w2 = __fdividef(b.p1.m, a1 * a1 * a1) + __fdividef(b.p2.m, a2 * a2 * a2);
+    return P.nu * cs2 * rsqrtf(w2) * P.inv_sqrt_gm;
+}
+
+// intercell_flux (physics.rs:584-607 iso, 776-803 euler) from the two cells'
+// primitive (pc), slope along the face normal (g) and stress terms: sn the
+// normal-normal shear term, st the off-diagonal one, bk the bulk term.
+template <int NF, int AXIS>
+__device__ __forceinline__ void face_flux(const DevParamsF& P, const Binary<float>& B, const float* pcl,
+                                          const float* gl, float snl, float stl, float bkl, const float* pcr,
+                                          const float* gr, float snr, float str, float bkr, float x, float y,
+                                          float* F)
+{
+    float pl[NF], pr[NF];
+#pragma unroll
+    for (int k = 0; k < NF; ++k) {
+        pl[k] = pcl[k] + 0.5f * gl[k];
+        pr[k] = pcr[k] - 0.5f * gr[k];
+    }
+    float lnu, rnu;
+    if (P.visc == 0) {
+        lnu = rnu = P.nu;
+    } else {
+        lnu = alpha_nu_f<NF>(P, B, x, y, pcl);
+        rnu = alpha_nu_f<NF>(P, B, x, y, pcr);
+    }
+    const float lam = P.lambda;
+    const float tn = 0.5f * (pcl[0] * (lnu * snl + lam * lnu * bkl) + pcr[0] * (rnu * snr + lam * rnu * bkr));
+    const float tt = 0.5f * (pcl[0] * (lnu * stl) + pcr[0] * (rnu * str));
+    const float tau_x = AXIS == 0 ? tn : tt;
+    const float tau_y = AXIS == 0 ? tt : tn;
+    float cs2 = 0.0f;
+    if constexpr (NF == 3) cs2 = -binary_potential(B, x, y, P.soft2) * P.inv_mach2;
+    hlle<NF, float>(P, pl, pr, AXIS, cs2, F);
+    F[1] -= tau_x;
+    F[2] -= tau_y;
+    if constexpr (NF == 4) F[3] -= tau_x * 0.5f * (pcl[1] + pcr[1]) + tau_y * 0.5f * (pcl[2] + pcr[2]);
+}
+
+// Source ledger items that can be non-zero (grav mass, isothermal cooling and
+// Euler fake mass are identically zero).
+template <int NF> __device__ __forceinline__ constexpr bool item_live(int k)
+{
+    const int item = k / NF, f = k % NF;
+    if ((item == GRAV1 || item == GRAV2) && f == 0) return false;
+    if (NF == 3 && item == COOLING) return false;
+    if (NF == 4 && item == FAKE_MASS) return false;
+    return true;
+}
+
+template <int NF, int STORE>
+__global__ void __launch_bounds__(160) stage2_kernel(StageArgs a)
+{
+    using E = typename std::conditional<STORE == 1, float, double>::type;
+    constexpr int H = STORE == 1 ? 4 : 2;     // staged halo columns per side: 16 bytes
+    constexpr int NL = NITEMS * NF;
+
+    const int TW = blockDim.x - 32;
+    const int TH = a.th;
+    const int t = threadIdx.x;
+    const int SW = TW + 2 * H;
+
+    int ri = 0;
+    const int g = blockIdx.x;
+    while (ri + 1 < a.nruns && g >= a.runs[ri + 1].tile_base) ++ri;
+    const RunDev& rd = a.runs[ri];
+    if (g - rd.tile_base >= rd.ntiles) return;
+
+    __shared__ DevParamsF P;
+    __shared__ Binary<float> B;
+    __shared__ double orbd[10];
+    __shared__ int failed, timeout;
+    if (t == 0) {
+        failed = (*(volatile unsigned long long*)a.err_key != ~0ull);
+        timeout = 0;
+    }
+    __syncthreads();
+    if (failed) return;
+    if (t == 0) P = rd.pf;
+    if (t < 10) orbd[t] = rd.orbit[a.stage * 10 + t];
+    __syncthreads();
+    if (t == 0) {
+        B.p1 = {(float)orbd[0], (float)orbd[1], (float)orbd[2], (float)orbd[3], (float)orbd[4]};
+        B.p2 = {(float)orbd[5], (float)orbd[6], (float)orbd[7], (float)orbd[8], (float)orbd[9]};
+    }
+
+    const int N = rd.N, bs = rd.bs;
+    const size_t nn = (size_t)N * N;
+    const int lt = g - rd.tile_base;
+    const int tj = lt % rd.tiles_j, ti = lt / rd.tiles_j;
+    const int i0 = ti * TH, j0 = tj * TW;
+    const int bi = i0 / bs, bj = j0 / bs, li0 = i0 % bs, lj0 = j0 % bs;
+    const int block = bi * rd.nb + bj;
+    const int tib = (li0 / TH) * (bs / TW) + lj0 / TW;
+    const bool has_base = a.base_slot >= 0;
+
+    const E* uin = (const E*)rd.slot[a.in_slot];
+    const E* ubase = has_base ? (const E*)rd.slot[a.base_slot] : nullptr;
+    E* uout = (E*)rd.slot[a.out_slot];
+    const E* ubg = (const E*)rd.bg;
+    const float dt = (float)*rd.dt;
+    const float time = (float)rd.stage_time[a.stage];
+    const float* xc = rd.xcf;
+    const float* xv = rd.xvf;
+
+    // ---- shared memory carve-up ------------------------------------------------
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    const int SLOT = s2_slot_bytes(NF, STORE, TW);
+    unsigned char* slots = smem_raw;
+    float4* sP = (float4*)(slots + S2_SLOTS * SLOT);         // [2][TW+4]  primitives of a row
+    float4* sR0 = sP + 2 * (TW + 4);                          // [2][TW+2]  cell record, 3 float4 planes
+    float4* sR1 = sR0 + 2 * (TW + 2);
+    float4* sR2 = sR1 + 2 * (TW + 2);
+    float4* sF = sR2 + 2 * (TW + 2);                          // [2][TW+1]  y-face fluxes
+    uint64_t* bars = (uint64_t*)(sF + 2 * (TW + 1));
+
+    // ---- roles -----------------------------------------------------------------
+    const bool interior = t < TW;
+    const int hl = t - TW;                                    // lane in the halo warp
+    const bool active = interior || (hl >= 0 && hl < 4);
+    const int c = interior ? t : (hl < 2 ? hl - 2 : TW + hl - 2);
+    const bool has_rec = active && c >= -1 && c <= TW;
+    const bool has_fy = active && c >= 0 && c <= TW;
+    const bool producer = (hl == 4);
+
+    // stencil plane of field f in the stage input (hi plane for the compensated store)
+    auto plane = [&](const E* base, int f, int part) -> const E* {
+        return STORE == 1 ? base + (size_t)(2 * f + part) * nn : base + (size_t)f * nn;
+    };
+
+    // ---- producer: stage tile row r into its slot -----------------------------------
+    auto copy_row = [&](unsigned char* dst, const E* row, int w_halo, uint64_t* bar) {
+        if (w_halo == 0) {
+            bulk_load(dst, row + j0, TW * sizeof(E), bar);
+        } else if (j0 >= H && j0 + TW + H <= N) {
+            bulk_load(dst, row + j0 - H, SW * sizeof(E), bar);
+        } else {
+            bulk_load(dst, row + (j0 - H + N) % N, H * sizeof(E), bar);
+            bulk_load(dst + H * sizeof(E), row + j0, TW * sizeof(E), bar);
+            bulk_load(dst + (H + TW) * sizeof(E), row + (j0 + TW) % N, H * sizeof(E), bar);
+        }
+    };
+    auto issue = [&](int r) {
+        const int rr = r + 2;
+        unsigned char* sb = slots + (rr % S2_SLOTS) * SLOT;
+        uint64_t* bar = bars + rr % S2_SLOTS;
+        const int gi = wrap(i0 + r, N);
+        const bool upd = r >= 0 && r < TH;
+        uint32_t bytes = NF * SW * sizeof(E);
+        if (upd) {
+            if (STORE == 1) bytes += (2 + (has_base ? 2 : 0)) * NF * TW * sizeof(E);
+            else bytes += (1 + (has_base ? 1 : 0)) * NF * TW * sizeof(E);
+        }
+        fence_proxy_async();
+        mbar_arrive_expect_tx(bar, bytes);
+        const size_t roff = (size_t)gi * N;
+        for (int f = 0; f < NF; ++f) copy_row(sb + f * SW * sizeof(E), plane(uin, f, 0) + roff, 1, bar);
+        if (upd) {
+            unsigned char* q = sb + NF * SW * sizeof(E);
+            if (STORE == 1) {
+                for (int f = 0; f < NF; ++f, q += TW * sizeof(E)) copy_row(q, plane(uin, f, 1) + roff, 0, bar);
+                for (int f = 0; f < NF; ++f, q += TW * sizeof(E)) copy_row(q, plane(ubg, f, 0) + roff, 0, bar);
+                if (has_base) {
+                    for (int f = 0; f < NF; ++f, q += TW * sizeof(E)) copy_row(q, plane(ubase, f, 0) + roff, 0, bar);
+                    for (int f = 0; f < NF; ++f, q += TW * sizeof(E)) copy_row(q, plane(ubase, f, 1) + roff, 0, bar);
+                }
+            } else {
+                for (int f = 0; f < NF; ++f, q += TW * sizeof(E)) copy_row(q, plane(ubg, f, 0) + roff, 0, bar);
+                if (has_base)
+                    for (int f = 0; f < NF; ++f, q += TW * sizeof(E)) copy_row(q, plane(ubase, f, 0) + roff, 0, bar);
+            }
+        }
+    };
+
+    if (producer) {
+        for (int s = 0; s < S2_SLOTS; ++s) mbar_init(bars + s, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    if (producer)
+        for (int r = -2; r < -2 + S2_DEPTH; ++r) issue(r);
+
+    const float theta = P.plm, pdt = P.pdt, inv_dx = P.inv_dx;
+
+    float Pm1[NF], P0[NF];               // primitives of rows rg-1, rg (own column)
+    float rxa[2 * NF + 3], rxb[2 * NF + 3];  // x-face records of rows rq, rq+1: pc, gx, sxx, sxy, bulk
+    float fxA[NF], fxB[NF];              // x fluxes at faces ru-1/2, ru+1/2
+    float led[NL];
+#pragma unroll
+    for (int k = 0; k < NL; ++k) led[k] = 0.0f;
+    float amax = 0.0f;
+#pragma unroll
+    for (int f = 0; f < NF; ++f) { Pm1[f] = P0[f] = fxA[f] = fxB[f] = 0.0f; }
+#pragma unroll
+    for (int w = 0; w < 2 * NF + 3; ++w) rxa[w] = rxb[w] = 0.0f;
+
+    for (int k = 0; k < TH + 5; ++k) {
+        const int rn = k - 2;
+        if (producer && rn + S2_DEPTH <= TH + 1) issue(rn + S2_DEPTH);
+
+        // ---- phase 1: row rn -> primitives (try_block_primitive, scheme.rs:185-199) --
+        float pn[NF];
+#pragma unroll
+        for (int f = 0; f < NF; ++f) pn[f] = 0.0f;
+        if (rn <= TH + 1 && active) {
+            const int rr = rn + 2;
+            uint64_t* bar = bars + rr % S2_SLOTS;
+            if (!mbar_wait_bounded(bar, (rr / S2_SLOTS) & 1)) timeout = 1;
+            const E* sb = (const E*)(slots + (rr % S2_SLOTS) * SLOT);
+            float u[NF];
+#pragma unroll
+            for (int f = 0; f < NF; ++f) u[f] = (float)sb[f * SW + c + H];
+            float bad = 0.0f;
+            int e = try_to_primitive<NF, float>(P, u, pn, bad);
+            if (e && interior && rn >= 0 && rn < TH) {
+                const int gi = i0 + rn;
+                atomicMin(a.err_key, error_key(a.stage, ri, rd, gi, j0 + c, e));
+            }
+            sP[(rn & 1) * (TW + 4) + c + 2] = make_float4(pn[0], pn[1], pn[2], NF == 4 ? pn[NF - 1] : 0.0f);
+        }
+
+        // ---- phase 2: slopes and cell record of row rg = rn - 1 (scheme.rs:216-254) ---
+        const int rg = rn - 1;
+        if (rg >= -1 && rg <= TH && has_rec) {
+            const float4 l4 = sP[(rg & 1) * (TW + 4) + c + 1];
+            const float4 r4 = sP[(rg & 1) * (TW + 4) + c + 3];
+            const float lv[4] = {l4.x, l4.y, l4.z, l4.w}, rv[4] = {r4.x, r4.y, r4.z, r4.w};
+            const float thx = (Pm1[0] < pdt || P0[0] < pdt || pn[0] < pdt) ? 0.0f : theta;
+            const float thy = (lv[0] < pdt || P0[0] < pdt || rv[0] < pdt) ? 0.0f : theta;
+            float gx[NF], gy[NF];
+#pragma unroll
+            for (int f = 0; f < NF; ++f) {
+                gx[f] = plm_gradient(thx, Pm1[f], P0[f], pn[f]);
+                gy[f] = plm_gradient(thy, lv[f], P0[f], rv[f]);
+            }
+            const float da = gx[1] * inv_dx, db = gy[2] * inv_dx;
+            const float sxx = (4.0f / 3.0f) * da - (2.0f / 3.0f) * db;
+            const float syy = (4.0f / 3.0f) * db - (2.0f / 3.0f) * da;
+            const float sxy = (gx[2] + gy[1]) * inv_dx;
+            const float bulk = da + db;
+            // y-face record for the right neighbour: pc | gy | sxy, syy, bulk
+            float yr[12];
+#pragma unroll
+            for (int f = 0; f < NF; ++f) { yr[f] = P0[f]; yr[NF + f] = gy[f]; }
+            yr[2 * NF] = sxy;
+            yr[2 * NF + 1] = syy;
+            yr[2 * NF + 2] = bulk;
+#pragma unroll
+            for (int w = 2 * NF + 3; w < 12; ++w) yr[w] = 0.0f;
+            const int o = (rg & 1) * (TW + 2) + c + 1;
+            sR0[o] = make_float4(yr[0], yr[1], yr[2], yr[3]);
+            sR1[o] = make_float4(yr[4], yr[5], yr[6], yr[7]);
+            sR2[o] = make_float4(yr[8], yr[9], yr[10], yr[11]);
+            // x-face record kept in registers
+#pragma unroll
+            for (int w = 0; w < 2 * NF + 3; ++w) rxa[w] = rxb[w];
+#pragma unroll
+            for (int f = 0; f < NF; ++f) { rxb[f] = P0[f]; rxb[NF + f] = gx[f]; }
+            rxb[2 * NF] = sxx;
+            rxb[2 * NF + 1] = sxy;
+            rxb[2 * NF + 2] = bulk;
+        }
+        if (rn <= TH + 1) {
+#pragma unroll
+            for (int f = 0; f < NF; ++f) { Pm1[f] = P0[f]; P0[f] = pn[f]; }
+        }
+
+        // ---- phase 3: x flux at face rq+1/2 and y fluxes of row rq = rn - 2 ---------
+        const int rq = rn - 2;
+        float fxn[NF];
+#pragma unroll
+        for (int f = 0; f < NF; ++f) fxn[f] = 0.0f;
+        if (interior && rq >= -1 && rq <= TH - 1) {
+            const float x = xv[bi * (bs + 1) + li0 + rq + 1];
+            const float y = xc[j0 + c];
+            face_flux<NF, 0>(P, B, rxa, rxa + NF, rxa[2 * NF], rxa[2 * NF + 1], rxa[2 * NF + 2], rxb, rxb + NF,
+                             rxb[2 * NF], rxb[2 * NF + 1], rxb[2 * NF + 2], x, y, fxn);
+        }
+        if (has_fy && rq >= 0 && rq <= TH - 1) {
+            const int ol = (rq & 1) * (TW + 2) + c, orr = ol + 1;
+            float L[12], Rr[12];
+            {
+                float4 v0 = sR0[ol], v1 = sR1[ol], v2 = sR2[ol];
+                L[0] = v0.x; L[1] = v0.y; L[2] = v0.z; L[3] = v0.w; L[4] = v1.x; L[5] = v1.y;
+                L[6] = v1.z; L[7] = v1.w; L[8] = v2.x; L[9] = v2.y; L[10] = v2.z; L[11] = v2.w;
+                float4 w0 = sR0[orr], w1 = sR1[orr], w2 = sR2[orr];
+                Rr[0] = w0.x; Rr[1] = w0.y; Rr[2] = w0.z; Rr[3] = w0.w; Rr[4] = w1.x; Rr[5] = w1.y;
+                Rr[6] = w1.z; Rr[7] = w1.w; Rr[8] = w2.x; Rr[9] = w2.y; Rr[10] = w2.z; Rr[11] = w2.w;
+            }
+            const float x = xc[i0 + rq];
+            const float y = xv[bj * (bs + 1) + lj0 + c];
+            float F[NF];
+            face_flux<NF, 1>(P, B, L, L + NF, L[2 * NF + 1], L[2 * NF], L[2 * NF + 2], Rr, Rr + NF, Rr[2 * NF + 1],
+                             Rr[2 * NF], Rr[2 * NF + 2], x, y, F);
+            sF[(rq & 1) * (TW + 1) + c] = make_float4(F[0], F[1], F[2], NF == 4 ? F[NF - 1] : 0.0f);
+        }
+
+        // ---- phase 4: update row ru = rn - 3 (scheme.rs:290-305, state.rs:183-199) -------
+        const int ru = rn - 3;
+        if (interior && ru >= 0 && ru <= TH - 1) {
+            const int rr = ru + 2;
+            const E* sb = (const E*)(slots + (rr % S2_SLOTS) * SLOT);
+            const float4 fl4 = sF[(ru & 1) * (TW + 1) + c], fr4 = sF[(ru & 1) * (TW + 1) + c + 1];
+            const float fyl[4] = {fl4.x, fl4.y, fl4.z, fl4.w}, fyr[4] = {fr4.x, fr4.y, fr4.z, fr4.w};
+            const int gi = i0 + ru, gj = j0 + c;
+            const float x = xc[gi], y = xc[gj];
+            float uc[NF], u0[NF];
+            const E* q = sb + NF * SW;
+#pragma unroll
+            for (int f = 0; f < NF; ++f) uc[f] = (float)sb[f * SW + c + H];
+            if (STORE == 1) {
+#pragma unroll
+                for (int f = 0; f < NF; ++f) u0[f] = (float)q[(NF + f) * TW + c];
+            } else {
+#pragma unroll
+                for (int f = 0; f < NF; ++f) u0[f] = (float)q[f * TW + c];
+            }
+            float it[NL];
+            source_terms<NF, float>(P, B, uc, u0, x, y, time, dt, it);
+            const size_t idx = (size_t)gi * N + gj;
+#pragma unroll
+            for (int f = 0; f < NF; ++f) {
+                float tot = it[SINK1 * NF + f] + it[SINK2 * NF + f] + it[GRAV1 * NF + f] + it[GRAV2 * NF + f] +
+                            it[BUFFER * NF + f] + it[COOLING * NF + f] + it[FAKE_MASS * NF + f];
+                float du = ((fxB[f] - fxA[f]) + (fyr[f] - fyl[f])) * inv_dx * -dt;
+                float inc = du + tot;
+                if constexpr (STORE == 1) {
+                    df32 o = df_add_f(df32{(float)sb[f * SW + c + H], (float)q[f * TW + c]}, inc);
+                    if (has_base) {
+                        df32 b0{(float)q[(2 * NF + f) * TW + c], (float)q[(3 * NF + f) * TW + c]};
+                        if (a.bf == 0.5) {
+                            df32 s = df_add(o, b0);
+                            o = {s.hi * 0.5f, s.lo * 0.5f};
+                        } else {
+                            o = df_add(df_mul(o, df32{a.w1f.hi, a.w1f.lo}), df_mul(b0, df32{a.bff.hi, a.bff.lo}));
+                        }
+                    }
+                    ((float*)uout)[(size_t)(2 * f) * nn + idx] = o.hi;
+                    ((float*)uout)[(size_t)(2 * f + 1) * nn + idx] = o.lo;
+                    if (a.amax_flag) uc[f] = o.hi;
+                } else {
+                    double o = (double)sb[f * SW + c + H] + (double)inc;
+                    if (has_base) o = o * (-a.bf + 1.0) + (double)q[(NF + f) * TW + c] * a.bf;
+                    ((double*)uout)[(size_t)f * nn + idx] = o;
+                    if (a.amax_flag) uc[f] = (float)o;
+                }
+            }
+#pragma unroll
+            for (int k2 = 0; k2 < NL; ++k2)
+                if (item_live<NF>(k2)) led[k2] += it[k2];
+            if (a.amax_flag) amax = fmaxf(max_signal_speed<NF, float>(P, uc), amax);
+        }
+        if (rq >= -1 && rq <= TH - 1) {
+#pragma unroll
+            for (int f = 0; f < NF; ++f) { fxA[f] = fxB[f]; fxB[f] = fxn[f]; }
+        }
+        __syncthreads();
+    }
+
+    // ---- per-tile ledger and max speed (deterministic tree over the CTA) -------------
+    double* red = (double*)smem_raw;
+    const int NT = blockDim.x;
+    for (int k = 0; k < NL; ++k) {
+        if (!item_live<NF>(k)) {
+            if (t == 0) rd.partial[((size_t)block * rd.tiles_per_block + tib) * NL + k] = 0.0;
+            continue;
+        }
+        red[t] = (double)led[k];
+        __syncthreads();
+        for (int s = 1; s < NT; s <<= 1) {
+            if ((t & (2 * s - 1)) == 0 && t + s < NT) red[t] += red[t + s];
+            __syncthreads();
+        }
+        if (t == 0) rd.partial[((size_t)block * rd.tiles_per_block + tib) * NL + k] = red[0];
+        __syncthreads();
+    }
+    if (a.amax_flag) {
+        red[t] = (double)amax;
+        __syncthreads();
+        for (int s = 1; s < NT; s <<= 1) {
+            if ((t & (2 * s - 1)) == 0 && t + s < NT) red[t] = fmax(red[t], red[t + s]);
+            __syncthreads();
+        }
+        if (t == 0 && red[0] > 0.0) atomicMax(rd.amax, (unsigned long long)__double_as_longlong(red[0]));
+    }
+    if (t == 0 && timeout) atomicOr(a.timeout_flag, 1u);
+
+    __shared__ int is_last;
+    if (t == 0) {
+        __threadfence();
+        unsigned prev = atomicAdd(rd.counter + block, 1u);
+        is_last = (prev == (unsigned)rd.tiles_per_block - 1);
+    }
+    __syncthreads();
+    if (is_last) {
+        __threadfence();
+        const double area = (double)rd.p.dx * rd.p.dx;
+        const double* lin = rd.ledger[a.in_slot] + (size_t)block * NL;
+        const double* lbase = has_base ? rd.ledger[a.base_slot] + (size_t)block * NL : nullptr;
+        double* lout = rd.ledger[a.out_slot] + (size_t)block * NL;
+        for (int k = t; k < NL; k += NT) {
+            double s = 0.0;
+            for (int q = 0; q < rd.tiles_per_block; ++q)
+                s += __ldcg(rd.partial + ((size_t)block * rd.tiles_per_block + q) * NL + k);
+            double v = __ldcg(lin + k) + s * area;
+            if (lbase) v = v * (-a.bf + 1.0) + __ldcg(lbase + k) * a.bf;
+            lout[k] = v;
+        }
+        if (t == 0) rd.counter[block] = 0u;
+    }
+}
+
+}  // namespace b2d

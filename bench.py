@@ -1,0 +1,391 @@
+"""Throughput benchmark: zone-updates/s of binary2d's RK step on one GB300.
+
+Workload (default): the isothermal circumbinary disk on 16x16 blocks of
+128^2 zones (2048^2), q = 1, e = 0, Mach 10, nu = 1e-3, PLM theta = 1.5,
+HLLE, RK2, CFL 0.4, synthetic initial state (Sigma = 1 with a cavity r < 2.5a,
+Keplerian velocity, seeded +-1e-3 noise).  One bench step is one advance
+(src/scheme.rs:323-349) with fold = 10 (setups/iso-circular.yaml:31): one dt,
+then 10 RK2 steps; zone-updates per step = 2048^2 x 10.  The state (100 MB)
+plus background exceed the 129 MB L2, so no flush is needed between steps.
+
+Arms:
+  --impl ours (default)  the CUDA path through the C ABI (libb2d.so)
+  --impl reference       the reference's CPU algorithm restated in C (the
+                         oracle port), all host threads, one RK step of the
+                         same mesh per bench step
+
+Under torchrun (N > 1) every rank advances its own disk (independent runs,
+weak scaling, no collective in the data path); timing is the max over ranks.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "app-binary2d_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np
+
+METRIC = "zone-updates/s: mixed-prec+batched vs plain FP64 on 1 GB300 at stated L1 err; %HBM"
+UNIT = "zone-updates/s"
+FOLD = 10
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Clocks:
+    """Sample nvidia-smi clocks and throttle reasons during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        mhz, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                mhz.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not mhz:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        return {"sm_mhz": statistics.median(mhz), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(mhz)}
+
+
+def cpu_sample(mesh, hydro, physics, model, seconds, nthreads):
+    """The oracle port on the host cores: RK steps of the same mesh for about
+    `seconds`; returns zone-updates/s."""
+    import binary2d as b2
+    from oracle import binding
+    cons = b2.initial_state(mesh, hydro, physics, model)
+    st = binding.OracleState(b2.to_c(mesh, hydro, physics), cons)
+    st.advance(1, nthreads=nthreads)  # warm
+    n, t0 = 0, time.perf_counter()
+    while True:
+        st.advance(1, nthreads=nthreads)
+        n += 1
+        el = time.perf_counter() - t0
+        if el >= seconds and n >= 2:
+            break
+    return mesh.total_zones() * n / el, n
+
+
+def reference_arm(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    import binary2d as b2
+    mesh, hydro, physics, model = b2.presets.disk_2048(seed=1)
+    nthreads = 2 * (os.cpu_count() or 1)   # the reference's default, src/app.rs:125-131
+    from oracle import binding
+    cons = b2.initial_state(mesh, hydro, physics, model)
+    st = binding.OracleState(b2.to_c(mesh, hydro, physics), cons)
+    for _ in range(args.warmup):
+        st.advance(1, nthreads=nthreads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        st.advance(1, nthreads=nthreads)
+    el = time.perf_counter() - t0
+    v = mesh.total_zones() * args.steps / el
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "iso disk 2048^2 (16x16 blocks of 128^2), one RK2 step per bench step",
+                   "global_batch": 1, "parallelism": "host threads"},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": nthreads, "kind": "port",
+                         "sample": "%d RK2 steps of the 2048^2 disk, %d threads on %d host cores"
+                                   % (args.steps, nthreads, os.cpu_count() or 1)},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def ours(args):
+    import torch
+    import binary2d as b2
+
+    ws, rank, local = dist_env()
+    dist = ws > 1
+    if dist:
+        import torch.distributed as tdist
+        torch.cuda.set_device(local)
+        tdist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    # libb2d has its own CUDA runtime: select the rank's device there too
+    b2.set_device(local if dist else 0)
+
+    if args.workload == "disk_2048":
+        mesh, hydro, physics, model = b2.presets.disk_2048(seed=1 + rank)
+        wname = "iso disk 2048^2 (16x16 blocks of 128^2), q=1 e=0 Mach 10, RK2, fold 10"
+    elif args.workload == "disk_512":
+        mesh, hydro, physics, model = b2.presets.disk_512(seed=1 + rank)
+        wname = "iso disk 512^2 (8x8 blocks of 64^2), q=1 e=0 Mach 10, RK2, fold 10"
+    elif args.workload == "disk_1024":
+        mesh, hydro, physics, model = b2.presets.iso_disk(8, 128, seed=1 + rank)
+        wname = "iso disk 1024^2 (8x8 blocks of 128^2)"
+    else:
+        raise SystemExit("unknown workload")
+    nf = 3
+    zones = mesh.total_zones()
+    cons = b2.initial_state(mesh, hydro, physics, model)
+    run = b2.Run(mesh, hydro, physics)
+
+    def make(prec):
+        rt = b2.Runtime([run], precision=prec)
+        if args.tile:
+            rt.set_tile(*[int(x) for x in args.tile.split("x")])
+        rt.upload(0, cons)
+        return rt
+
+    def barrier():
+        if dist:
+            torch.distributed.barrier()
+
+    def timed(rt, steps, warmup):
+        stream = torch.cuda.ExternalStream(rt.stream())
+        for _ in range(warmup):
+            rt.advance_async(FOLD)
+        rt.synchronize()
+        barrier()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        l0 = rt.launch_count()
+        e0.record(stream)
+        for _ in range(steps):
+            rt.advance_async(FOLD)
+        e1.record(stream)
+        e1.synchronize()
+        rt.synchronize()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        launches = rt.launch_count() - l0
+        if dist:
+            t = torch.tensor([ms], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+        barrier()
+        return ms, launches
+
+    prec = args.precision
+    w = 8  # stored bytes per conserved word (FP64, or FP32 + FP32 compensation)
+    bytes_per_zone_update = 7 * nf * w          # RK2: 3 reads + 1 write, 2 reads + 1 write ... see the design doc
+    hbm_peak, peak_kind = peaks()
+
+    rt = make(prec)
+    with Clocks(local) as clk:
+        ms, launches = timed(rt, args.steps, args.warmup)
+    value = zones * FOLD * args.steps / (ms / 1e3) * ws
+
+    # dominant kernel: average stage-kernel duration over an instrumented pass
+    rt.set_instrument(True)
+    for _ in range(max(2, args.steps // 4)):
+        rt.advance(FOLD)
+    nst, st_ms = rt.stage_stats()
+    rt.set_instrument(False)
+    stage_ms = st_ms / max(nst, 1)
+    bytes_per_launch = bytes_per_zone_update / 2.0 * zones      # average of the two RK2 stages
+    achieved = bytes_per_launch / (stage_ms / 1e3) / 1e9
+    rt.close()
+
+    # plain FP64 on the same workload (shorter)
+    fp64_value = None
+    if prec != "fp64" and not args.skip_fp64:
+        rt64 = make("fp64")
+        ms64, _ = timed(rt64, max(2, args.steps // 5), 2)
+        fp64_value = zones * FOLD * max(2, args.steps // 5) / (ms64 / 1e3) * ws
+        rt64.close()
+
+    # end to end through the C ABI with pinned host buffers: upload the
+    # state, advance, download the state, every step
+    host_in = np.ascontiguousarray(cons.copy())
+    host_out = np.empty_like(host_in)
+    b2.pin(host_in)
+    b2.pin(host_out)
+    rt = make(prec)
+    for _ in range(2):
+        rt.upload_conserved(0, host_in)
+        rt.advance(FOLD)
+        rt.download(0, out=host_out)
+    barrier()
+    e2e_steps = max(3, args.steps // 2)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        rt.upload_conserved(0, host_in)
+        rt.advance(FOLD)
+        rt.download(0, out=host_out)
+    el = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([el], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        el = float(t.item())
+    e2e_value = zones * FOLD * e2e_steps / el * ws
+    rt.close()
+    b2.unpin(host_in)
+    b2.unpin(host_out)
+
+    # accuracy of the mixed path against the FP64 path (512^2 disk, 1/4 orbit)
+    accuracy = None
+    if prec != "fp64" and not args.skip_accuracy and rank == 0:
+        accuracy = accuracy_check(prec, orbits=args.accuracy_orbits)
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.skip_cpu:
+        nthreads = 2 * (os.cpu_count() or 1)
+        v, n = cpu_sample(mesh, hydro, physics, model, args.cpu_seconds, nthreads)
+        cpu = {"value": v, "unit": UNIT, "cores": nthreads, "kind": "port",
+               "sample": "%d RK2 steps of the same 2048^2 disk with the C oracle, %d threads on %d host cores"
+                         % (n, nthreads, os.cpu_count() or 1)}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": {"fp64": "f64", "fp32_state64": "f32 (f64 state)",
+                                                             "fp32_comp": "f32 (compensated f32 state)"}[prec],
+            "data": "synthetic",
+            "config": {"workload": wname, "precision": prec, "zones": zones, "fold": FOLD,
+                       "global_batch": ws, "parallelism": "replicas" if ws > 1 else "single GPU",
+                       "l2": "state + background > L2 (no flush needed)",
+                       "tile": "%dx%d" % tuple(make_tile_info(args, run, prec))},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": achieved / hbm_peak, "peak_kind": peak_kind, "traffic": None,
+                         "bytes_per_zone_update": bytes_per_zone_update, "stage_ms": stage_ms},
+            "fp64": {"value": fp64_value, "ratio": (value / fp64_value) if fp64_value else None},
+            "accuracy": accuracy,
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(cons.nbytes),
+                    "d2h_bytes_per_step": int(cons.nbytes)},
+            "gpu_launches": int(launches),
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line))
+    if dist:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def make_tile_info(args, run, prec):
+    import binary2d as b2
+    rt = b2.Runtime([run], precision=prec)
+    if args.tile:
+        rt.set_tile(*[int(x) for x in args.tile.split("x")])
+    t = rt.tile()
+    rt.close()
+    return t
+
+
+def accuracy_check(prec, orbits):
+    """Relative L1 error of Sigma and of the accreted mass (sink ledger) of the
+    mixed path against the FP64 path on the 512^2 disk after `orbits` orbits
+    (the FP64 run sets the number of advances)."""
+    import binary2d as b2
+    mesh, hydro, physics, model = b2.presets.disk_512(seed=1)
+    cons = b2.initial_state(mesh, hydro, physics, model)
+    out = {}
+    advances = None
+    for p in ("fp64", prec):
+        with b2.Runtime([b2.Run(mesh, hydro, physics)], precision=p) as rt:
+            rt.upload(0, cons)
+            n = 0
+            while (advances is None and rt.time(0)[0] < orbits * 2 * np.pi) or (advances is not None and n < advances):
+                rt.advance(FOLD)
+                n += 1
+            advances = n
+            s, t, _ = rt.download(0)
+            led = rt.ledger(0)
+        out[p] = (s, led, t)
+    s64, led64, t64 = out["fp64"]
+    s32, led32, _ = out[prec]
+    l1 = float(np.abs(s32[..., 0] - s64[..., 0]).sum() / np.abs(s64[..., 0]).sum())
+    acc64 = led64[:, :, 0:2, 0].sum()
+    acc32 = led32[:, :, 0:2, 0].sum()
+    return {"workload": "iso disk 512^2", "steps": advances * FOLD, "orbits": t64 / (2 * np.pi),
+            "l1_sigma_rel": l1, "accreted_mass_rel": float(abs(acc32 - acc64) / abs(acc64)) if acc64 else None,
+            "reference": "FP64 GPU path (matches the CPU oracle to 1e-12)"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp32_comp", choices=["fp64", "fp32_state64", "fp32_comp"])
+    ap.add_argument("--workload", default="disk_2048")
+    ap.add_argument("--tile", default="")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--accuracy-orbits", type=float, default=1.0)
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-fp64", action="store_true")
+    ap.add_argument("--skip-accuracy", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    if args.impl == "reference":
+        return reference_arm(args)
+    return ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -247,10 +247,27 @@ int64_t b2d_launch_count(const b2d_ctx* ctx);
 /* Launches per advance of `fold` steps (for reporting). */
 int64_t b2d_launches_per_advance(const b2d_ctx* ctx, int32_t fold);
 
-/* Average device time of the stage kernel in the last timed window (ms), as
- * measured with CUDA events on the context's stream; see b2d_time_stages. */
+/* Run `reps` advances of `fold` steps with CUDA events recorded around every
+ * stage-kernel launch on the context's stream; returns the average stage
+ * kernel duration in ms. */
 b2d_status b2d_time_stages(b2d_ctx* ctx, int32_t fold, int32_t reps,
                            double* ms_per_stage);
+
+/* Event instrumentation of subsequent advances (graphs are bypassed while
+ * on); b2d_stage_stats reports the stage launches timed and their total ms. */
+b2d_status b2d_set_instrument(b2d_ctx* ctx, int32_t enable);
+b2d_status b2d_stage_stats(const b2d_ctx* ctx, int64_t* count, double* total_ms);
+
+/* The context's CUDA stream (a cudaStream_t), for event timing by callers. */
+b2d_status b2d_stream(const b2d_ctx* ctx, void** stream);
+
+/* Page-lock / release a caller-owned host buffer (cudaHostRegister) so that
+ * uploads and downloads from it are DMA transfers. */
+b2d_status b2d_pin_host(void* ptr, uint64_t bytes);
+b2d_status b2d_unpin_host(void* ptr);
+
+/* Select the CUDA device used by contexts created afterwards on this thread. */
+b2d_status b2d_set_device(int32_t device);
 
 #ifdef __cplusplus
 }

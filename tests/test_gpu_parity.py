@@ -110,8 +110,46 @@ def test_tiny_blocks_and_small_tiles():
     """Blocks smaller than a warp (4x4 blocks of 8^2) exercise the periodic
     halo across many block edges."""
     mesh, hydro, physics, model = b2.presets.iso_disk(4, 8, seed=8)
+    physics = dataclasses.replace(physics, buffer_rate=10.0)
     r = run_pair(mesh, hydro, physics, model, fold=5, advances=2)
     check(r)
+
+
+def test_failure_is_the_reference_error():
+    """At dx = 0.5 the explicit buffer (rate 1000) drives a zone negative.
+    Both sides reject the step, and the GPU names the zone the reference
+    would: first block in index order with a failing 3x3 neighbour, its
+    first failing neighbour, that block's first failing zone."""
+    mesh, hydro, physics, model = b2.presets.iso_disk(4, 8, seed=8)
+    cons, cfg = make_case(mesh, hydro, physics, model)
+    ref = binding.OracleState(cfg, cons)
+    with b2.Runtime([b2.Run(mesh, hydro, physics)]) as rt:
+        rt.upload(0, cons)
+        gpu_err = None
+        for _ in range(4):
+            try:
+                rt.advance(5)
+            except b2.HydroError as e:
+                gpu_err = e
+                break
+        assert gpu_err is not None
+        out, t, it = rt.download(0)
+    ref_err = None
+    for _ in range(4):
+        try:
+            ref.advance(5)
+        except binding.OracleHydroError as e:
+            ref_err = e.err
+            break
+    assert ref_err is not None
+    assert gpu_err.code == ref_err.code
+    assert gpu_err.block == (ref_err.block_i, ref_err.block_j)
+    assert gpu_err.zone == (ref_err.zone_i, ref_err.zone_j)
+    assert gpu_err.position == (ref_err.x, ref_err.y)
+    assert abs(gpu_err.value - ref_err.value) <= 1e-12 * abs(ref_err.value)
+    assert abs(gpu_err.time - ref_err.time) <= 1e-12 * abs(ref_err.time)
+    # the GPU context is left at the state before the failing advance
+    assert rel_err(out, ref.cons) <= TOL and it == ref.iteration.value
 
 
 def test_background_differs_from_state():
