@@ -185,6 +185,12 @@ class Runtime:
         _check(self.lib.b2d_get_tile(self.ctx, ctypes.byref(w), ctypes.byref(h)))
         return w.value, h.value
 
+    def autotune(self, fold: int = 2, reps: int = 2):
+        """Pick the fastest tile shape for this context; returns (w, h, ms/stage)."""
+        w, h, ms = ctypes.c_int32(0), ctypes.c_int32(0), ctypes.c_double(0)
+        _check(self.lib.b2d_autotune(self.ctx, fold, reps, ctypes.byref(w), ctypes.byref(h), ctypes.byref(ms)))
+        return w.value, h.value, ms.value
+
     def set_graphs(self, on: bool):
         _check(self.lib.b2d_set_graphs(self.ctx, int(bool(on))))
 

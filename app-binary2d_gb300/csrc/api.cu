@@ -1036,3 +1036,78 @@ extern "C" b2d_status b2d_set_device(int32_t device)
     CUDA_TRY(cudaSetDevice(device));
     return B2D_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Tile autotuner: time every tile shape that divides the block size with CUDA
+// events on the context's stream, keep the fastest.  The advances run from
+// the current slot, which the slot schedule never overwrites, so the state is
+// unchanged afterwards (the max signal speed is recomputed).
+static b2d_status time_tile(b2d_ctx* ctx, int fold, int reps, double* ms)
+{
+    ctx->instrument = true;
+    ctx->stage_ms_total = 0.0;
+    ctx->stage_count = 0;
+    for (int r = 0; r < reps + 1; ++r) {
+        int fs;
+        std::vector<StagePlan> plan = plan_advance(ctx->rk, fold, ctx->cur, &fs);
+        b2d_status st = enqueue_advance(ctx, fold, ctx->cur, &fs, true);
+        if (st != B2D_OK) { ctx->instrument = false; return st; }
+        CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+        if (r == 0) continue;  // warm-up
+        for (size_t s = 0; s < plan.size(); ++s) {
+            float m = 0;
+            CUDA_TRY(cudaEventElapsedTime(&m, ctx->ev[2 * s], ctx->ev[2 * s + 1]));
+            ctx->stage_ms_total += m;
+            ctx->stage_count++;
+        }
+    }
+    ctx->instrument = false;
+    *ms = ctx->stage_ms_total / std::max<long long>(ctx->stage_count, 1);
+    return B2D_OK;
+}
+
+extern "C" b2d_status b2d_autotune(b2d_ctx* ctx, int32_t fold, int32_t reps, int32_t* tile_w, int32_t* tile_h,
+                                   double* ms_per_stage)
+{
+    if (!ctx || fold < 1 || reps < 1) return fail(B2D_ERR_INVALID, "bad arguments");
+    b2d_status st = ensure_stage_capacity(ctx, fold);
+    if (st != B2D_OK) return st;
+    CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    const int max_w = ctx->precision == B2D_PREC_FP64 ? 256 : 128;
+    int best_w = ctx->tw, best_h = ctx->th;
+    double best = 1e300;
+    for (int w : {32, 64, 128, 256}) {
+        if (w > max_w) continue;
+        for (int h : {8, 16, 32, 64, 128}) {
+            if (!tile_ok(ctx, w, h)) continue;
+            ctx->tw = w;
+            ctx->th = h;
+            st = sync_rundev(ctx);
+            if (st != B2D_OK) return st;
+            double ms = 0;
+            st = time_tile(ctx, fold, reps, &ms);
+            if (st != B2D_OK) return st;
+            if (ms < best) { best = ms; best_w = w; best_h = h; }
+        }
+    }
+    // discard what the trial advances left behind
+    long long count = 0;
+    CUDA_TRY(cudaMemcpy(&count, ctx->d_adv_count, sizeof count, cudaMemcpyDeviceToHost));
+    ctx->adv_base = count;
+    ctx->window.clear();
+    CUDA_TRY(cudaMemset(ctx->d_err_key, 0xff, sizeof(unsigned long long)));
+    CUDA_TRY(cudaMemset(ctx->d_timeout, 0, sizeof(unsigned)));
+    ctx->tw = best_w;
+    ctx->th = best_h;
+    st = sync_rundev(ctx);
+    if (st != B2D_OK) return st;
+    for (int r = 0; r < ctx->nruns; ++r) {
+        st = launch_max_speed(ctx, r, ctx->cur);
+        if (st != B2D_OK) return st;
+    }
+    CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    if (tile_w) *tile_w = best_w;
+    if (tile_h) *tile_h = best_h;
+    if (ms_per_stage) *ms_per_stage = best;
+    return B2D_OK;
+}

@@ -234,6 +234,15 @@ __global__ void __launch_bounds__(160) stage2_kernel(StageArgs a)
         for (int r = -2; r < -2 + S2_DEPTH; ++r) issue(r);
 
     const float theta = P.plm, pdt = P.pdt, inv_dx = P.inv_dx;
+    const bool half_avg = a.bf == 0.5;                  // RK2: (u + u0) / 2
+    const df32 w1{a.w1f.hi, a.w1f.lo}, wb{a.bff.hi, a.bff.lo};
+    const double bf = a.bf, w1d = -a.bf + 1.0;
+    const bool want_amax = a.amax_flag != 0;
+    // positions of this thread's column: zone centre y and left y-face
+    const float yc_own = interior ? xc[j0 + c] : 0.0f;
+    const float yv_own = has_fy ? xv[bj * (bs + 1) + lj0 + c] : 0.0f;
+    const float* xv_row = xv + bi * (bs + 1) + li0;    // x of face (i0 + r) - 1/2 is xv_row[r]
+    const float* xc_row = xc + i0;
 
     float Pm1[NF], P0[NF];               // primitives of rows rg-1, rg (own column)
     float rxa[2 * NF + 3], rxb[2 * NF + 3];  // x-face records of rows rq, rq+1: pc, gx, sxx, sxy, bulk
@@ -318,92 +327,93 @@ __global__ void __launch_bounds__(160) stage2_kernel(StageArgs a)
             for (int f = 0; f < NF; ++f) { Pm1[f] = P0[f]; P0[f] = pn[f]; }
         }
 
-        // ---- phase 3: x flux at face rq+1/2 and y fluxes of row rq = rn - 2 ---------
+        // ---- phases 3 and 4 -------------------------------------------------------------
+        // y flux of row rq = rn - 2 (this column's left face), update of row ru = rn - 3 and
+        // x flux of face rq + 1/2 (scheme.rs:257-268, 290-305; state.rs:183-199).  Interior
+        // threads run all three every iteration as one straight-line block (row indices
+        // clamped, side effects masked) so the compiler can interleave the independent
+        // dependency chains; the halo lane of column TW runs the y flux only.
         const int rq = rn - 2;
-        float fxn[NF];
-#pragma unroll
-        for (int f = 0; f < NF; ++f) fxn[f] = 0.0f;
-        if (interior && rq >= -1 && rq <= TH - 1) {
-            const float x = xv[bi * (bs + 1) + li0 + rq + 1];
-            const float y = xc[j0 + c];
-            face_flux<NF, 0>(P, B, rxa, rxa + NF, rxa[2 * NF], rxa[2 * NF + 1], rxa[2 * NF + 2], rxb, rxb + NF,
-                             rxb[2 * NF], rxb[2 * NF + 1], rxb[2 * NF + 2], x, y, fxn);
-        }
-        if (has_fy && rq >= 0 && rq <= TH - 1) {
+        const int ru = rn - 3;
+        const bool fy_ok = rq >= 0 && rq <= TH - 1;
+        const bool fx_ok = rq >= -1 && rq <= TH - 1;
+        const bool up_ok = ru >= 0 && ru <= TH - 1;
+        auto y_flux = [&]() {
             const int ol = (rq & 1) * (TW + 2) + c, orr = ol + 1;
-            float L[12], Rr[12];
-            {
-                float4 v0 = sR0[ol], v1 = sR1[ol], v2 = sR2[ol];
-                L[0] = v0.x; L[1] = v0.y; L[2] = v0.z; L[3] = v0.w; L[4] = v1.x; L[5] = v1.y;
-                L[6] = v1.z; L[7] = v1.w; L[8] = v2.x; L[9] = v2.y; L[10] = v2.z; L[11] = v2.w;
-                float4 w0 = sR0[orr], w1 = sR1[orr], w2 = sR2[orr];
-                Rr[0] = w0.x; Rr[1] = w0.y; Rr[2] = w0.z; Rr[3] = w0.w; Rr[4] = w1.x; Rr[5] = w1.y;
-                Rr[6] = w1.z; Rr[7] = w1.w; Rr[8] = w2.x; Rr[9] = w2.y; Rr[10] = w2.z; Rr[11] = w2.w;
-            }
-            const float x = xc[i0 + rq];
-            const float y = xv[bj * (bs + 1) + lj0 + c];
+            const float4 v0 = sR0[ol], v1 = sR1[ol], v2 = sR2[ol];
+            const float4 w0 = sR0[orr], w1v = sR1[orr], w2 = sR2[orr];
+            const float L[12] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w, v2.x, v2.y, v2.z, v2.w};
+            const float Rr[12] = {w0.x, w0.y, w0.z, w0.w, w1v.x, w1v.y, w1v.z, w1v.w, w2.x, w2.y, w2.z, w2.w};
+            const float x = xc_row[min(max(rq, 0), TH - 1)];
             float F[NF];
             face_flux<NF, 1>(P, B, L, L + NF, L[2 * NF + 1], L[2 * NF], L[2 * NF + 2], Rr, Rr + NF, Rr[2 * NF + 1],
-                             Rr[2 * NF], Rr[2 * NF + 2], x, y, F);
-            sF[(rq & 1) * (TW + 1) + c] = make_float4(F[0], F[1], F[2], NF == 4 ? F[NF - 1] : 0.0f);
-        }
+                             Rr[2 * NF], Rr[2 * NF + 2], x, yv_own, F);
+            if (fy_ok) sF[(rq & 1) * (TW + 1) + c] = make_float4(F[0], F[1], F[2], NF == 4 ? F[NF - 1] : 0.0f);
+        };
+        float fxn[NF];
+        if (interior) {
+            y_flux();
 
-        // ---- phase 4: update row ru = rn - 3 (scheme.rs:290-305, state.rs:183-199) -------
-        const int ru = rn - 3;
-        if (interior && ru >= 0 && ru <= TH - 1) {
-            const int rr = ru + 2;
-            const E* sb = (const E*)(slots + (rr % S2_SLOTS) * SLOT);
-            const float4 fl4 = sF[(ru & 1) * (TW + 1) + c], fr4 = sF[(ru & 1) * (TW + 1) + c + 1];
-            const float fyl[4] = {fl4.x, fl4.y, fl4.z, fl4.w}, fyr[4] = {fr4.x, fr4.y, fr4.z, fr4.w};
-            const int gi = i0 + ru, gj = j0 + c;
-            const float x = xc[gi], y = xc[gj];
-            float uc[NF], u0[NF];
-            const E* q = sb + NF * SW;
+            // update of row ru
+            {
+                const int rc = min(max(ru, 0), TH - 1);
+                const E* sb = (const E*)(slots + ((rc + 2) % S2_SLOTS) * SLOT);
+                const float4 fl4 = sF[(ru & 1) * (TW + 1) + c], fr4 = sF[(ru & 1) * (TW + 1) + c + 1];
+                const float fyl[4] = {fl4.x, fl4.y, fl4.z, fl4.w}, fyr[4] = {fr4.x, fr4.y, fr4.z, fr4.w};
+                const float x = xc_row[rc];
+                float uc[NF], u0[NF];
+                const E* q = sb + NF * SW;
 #pragma unroll
-            for (int f = 0; f < NF; ++f) uc[f] = (float)sb[f * SW + c + H];
-            if (STORE == 1) {
-#pragma unroll
-                for (int f = 0; f < NF; ++f) u0[f] = (float)q[(NF + f) * TW + c];
-            } else {
-#pragma unroll
-                for (int f = 0; f < NF; ++f) u0[f] = (float)q[f * TW + c];
-            }
-            float it[NL];
-            source_terms<NF, float>(P, B, uc, u0, x, y, time, dt, it);
-            const size_t idx = (size_t)gi * N + gj;
-#pragma unroll
-            for (int f = 0; f < NF; ++f) {
-                float tot = it[SINK1 * NF + f] + it[SINK2 * NF + f] + it[GRAV1 * NF + f] + it[GRAV2 * NF + f] +
-                            it[BUFFER * NF + f] + it[COOLING * NF + f] + it[FAKE_MASS * NF + f];
-                float du = ((fxB[f] - fxA[f]) + (fyr[f] - fyl[f])) * inv_dx * -dt;
-                float inc = du + tot;
-                if constexpr (STORE == 1) {
-                    df32 o = df_add_f(df32{(float)sb[f * SW + c + H], (float)q[f * TW + c]}, inc);
-                    if (has_base) {
-                        df32 b0{(float)q[(2 * NF + f) * TW + c], (float)q[(3 * NF + f) * TW + c]};
-                        if (a.bf == 0.5) {
-                            df32 s = df_add(o, b0);
-                            o = {s.hi * 0.5f, s.lo * 0.5f};
-                        } else {
-                            o = df_add(df_mul(o, df32{a.w1f.hi, a.w1f.lo}), df_mul(b0, df32{a.bff.hi, a.bff.lo}));
-                        }
-                    }
-                    ((float*)uout)[(size_t)(2 * f) * nn + idx] = o.hi;
-                    ((float*)uout)[(size_t)(2 * f + 1) * nn + idx] = o.lo;
-                    if (a.amax_flag) uc[f] = o.hi;
-                } else {
-                    double o = (double)sb[f * SW + c + H] + (double)inc;
-                    if (has_base) o = o * (-a.bf + 1.0) + (double)q[(NF + f) * TW + c] * a.bf;
-                    ((double*)uout)[(size_t)f * nn + idx] = o;
-                    if (a.amax_flag) uc[f] = (float)o;
+                for (int f = 0; f < NF; ++f) {
+                    uc[f] = (float)sb[f * SW + c + H];
+                    u0[f] = STORE == 1 ? (float)q[(NF + f) * TW + c] : (float)q[f * TW + c];
                 }
-            }
+                float it[NL];
+                source_terms<NF, float>(P, B, uc, u0, x, yc_own, time, dt, it);
+                const size_t idx = (size_t)(i0 + rc) * N + (j0 + c);
 #pragma unroll
-            for (int k2 = 0; k2 < NL; ++k2)
-                if (item_live<NF>(k2)) led[k2] += it[k2];
-            if (a.amax_flag) amax = fmaxf(max_signal_speed<NF, float>(P, uc), amax);
+                for (int f = 0; f < NF; ++f) {
+                    float tot = it[SINK1 * NF + f] + it[SINK2 * NF + f] + it[GRAV1 * NF + f] + it[GRAV2 * NF + f] +
+                                it[BUFFER * NF + f] + it[COOLING * NF + f] + it[FAKE_MASS * NF + f];
+                    float du = ((fxB[f] - fxA[f]) + (fyr[f] - fyl[f])) * inv_dx * -dt;
+                    float inc = du + tot;
+                    if constexpr (STORE == 1) {
+                        df32 o = df_add_f(df32{(float)sb[f * SW + c + H], (float)q[f * TW + c]}, inc);
+                        if (has_base) {
+                            df32 b0{(float)q[(2 * NF + f) * TW + c], (float)q[(3 * NF + f) * TW + c]};
+                            if (half_avg) {
+                                df32 sm = df_add(o, b0);
+                                o = {sm.hi * 0.5f, sm.lo * 0.5f};
+                            } else {
+                                o = df_add(df_mul(o, w1), df_mul(b0, wb));
+                            }
+                        }
+                        if (up_ok) {
+                            ((float*)uout)[(size_t)(2 * f) * nn + idx] = o.hi;
+                            ((float*)uout)[(size_t)(2 * f + 1) * nn + idx] = o.lo;
+                        }
+                        uc[f] = o.hi;
+                    } else {
+                        double o = (double)sb[f * SW + c + H] + (double)inc;
+                        if (has_base) o = o * w1d + (double)q[(NF + f) * TW + c] * bf;
+                        if (up_ok) ((double*)uout)[(size_t)f * nn + idx] = o;
+                        uc[f] = (float)o;
+                    }
+                }
+#pragma unroll
+                for (int k2 = 0; k2 < NL; ++k2)
+                    if (item_live<NF>(k2)) led[k2] += up_ok ? it[k2] : 0.0f;
+                if (want_amax && up_ok) amax = fmaxf(max_signal_speed<NF, float>(P, uc), amax);
+            }
+
+            // x flux of face rq + 1/2
+            face_flux<NF, 0>(P, B, rxa, rxa + NF, rxa[2 * NF], rxa[2 * NF + 1], rxa[2 * NF + 2], rxb, rxb + NF,
+                             rxb[2 * NF], rxb[2 * NF + 1], rxb[2 * NF + 2], xv_row[min(max(rq + 1, 0), TH)], yc_own,
+                             fxn);
+        } else if (hl == 2 && fy_ok) {
+            y_flux();
         }
-        if (rq >= -1 && rq <= TH - 1) {
+        if (fx_ok) {
 #pragma unroll
             for (int f = 0; f < NF; ++f) { fxA[f] = fxB[f]; fxB[f] = fxn[f]; }
         }

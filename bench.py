@@ -191,11 +191,18 @@ def ours(args):
     cons = b2.initial_state(mesh, hydro, physics, model)
     run = b2.Run(mesh, hydro, physics)
 
+    tuned = {}
+
     def make(prec):
         rt = b2.Runtime([run], precision=prec)
+        rt.upload(0, cons)
         if args.tile:
             rt.set_tile(*[int(x) for x in args.tile.split("x")])
-        rt.upload(0, cons)
+        elif prec in tuned:
+            rt.set_tile(*tuned[prec])
+        else:
+            w, h, _ = rt.autotune(fold=2, reps=2)
+            tuned[prec] = (w, h)
         return rt
 
     def barrier():
@@ -307,7 +314,8 @@ def ours(args):
             "config": {"workload": wname, "precision": prec, "zones": zones, "fold": FOLD,
                        "global_batch": ws, "parallelism": "replicas" if ws > 1 else "single GPU",
                        "l2": "state + background > L2 (no flush needed)",
-                       "tile": "%dx%d" % tuple(make_tile_info(args, run, prec))},
+                       "tile": "%dx%d" % tuned.get(prec, (0, 0)) if not args.tile else args.tile,
+                       "tile_source": "autotuner" if not args.tile else "--tile"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                          "frac": achieved / hbm_peak, "peak_kind": peak_kind, "traffic": None,
                          "bytes_per_zone_update": bytes_per_zone_update, "stage_ms": stage_ms},

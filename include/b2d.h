@@ -238,6 +238,13 @@ b2d_status b2d_initial_state(const b2d_config* cfg, const b2d_disk_model* model,
 b2d_status b2d_set_tile(b2d_ctx* ctx, int32_t tile_w, int32_t tile_h);
 b2d_status b2d_get_tile(const b2d_ctx* ctx, int32_t* tile_w, int32_t* tile_h);
 
+/* Tile autotuner: times every tile shape that divides the block size (width
+ * 32..128, or 256 for FP64; height 8..128) over `reps` advances of `fold`
+ * steps with CUDA events, keeps the fastest and reports it.  The context's
+ * state is unchanged. */
+b2d_status b2d_autotune(b2d_ctx* ctx, int32_t fold, int32_t reps, int32_t* tile_w,
+                        int32_t* tile_h, double* ms_per_stage);
+
 /* Use (1) or bypass (0) CUDA-graph replay of advance. Default 1. */
 b2d_status b2d_set_graphs(b2d_ctx* ctx, int32_t enable);
 
