@@ -140,7 +140,7 @@ template <int NF, class R> __device__ __forceinline__ void cons_to_prim_raw(cons
         p[2] = u[2] / u[0];
         if constexpr (NF == 4) p[3] = (u[3] - 0.5 * u[0] * (p[1] * p[1] + p[2] * p[2])) * P.gm1;
     } else {
-        float ir = __frcp_rn(u[0]);
+        float ir = __fdividef(1.0f, u[0]);
         p[1] = u[1] * ir;
         p[2] = u[2] * ir;
         if constexpr (NF == 4) p[3] = (u[3] - 0.5f * u[0] * (p[1] * p[1] + p[2] * p[2])) * P.gm1;
@@ -232,7 +232,7 @@ __device__ __forceinline__ void hlle(const DevParamsT<R>& P, const R* pl, const 
 #pragma unroll
         for (int k = 0; k < NF; ++k) F[k] = (fl[k] * ap - fr[k] * am - (ul[k] - ur[k]) * ap * am) / (ap - am);
     } else {
-        float inv = __frcp_rn(ap - am);
+        float inv = __fdividef(1.0f, ap - am);
         float apam = ap * am;
 #pragma unroll
         for (int k = 0; k < NF; ++k) F[k] = (fl[k] * ap - fr[k] * am - (ul[k] - ur[k]) * apam) * inv;

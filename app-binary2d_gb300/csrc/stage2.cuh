@@ -400,6 +400,7 @@ __global__ void __launch_bounds__(160) stage2_kernel(StageArgs a)
                         uc[f] = (float)o;
                     }
                 }
+                // a select, not a multiply by 0: the masked iterations may carry non-finite values
 #pragma unroll
                 for (int k2 = 0; k2 < NL; ++k2)
                     if (item_live<NF>(k2)) led[k2] += up_ok ? it[k2] : 0.0f;
