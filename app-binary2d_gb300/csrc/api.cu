@@ -10,6 +10,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -1110,4 +1111,187 @@ extern "C" b2d_status b2d_autotune(b2d_ctx* ctx, int32_t fold, int32_t reps, int
     if (tile_h) *tile_h = best_h;
     if (ms_per_stage) *ms_per_stage = best;
     return B2D_OK;
+}
+
+// ---------------------------------------------------------------------------
+// One RK stage that allocates nothing.
+//
+// Some callers cannot call cudaMalloc: a host code that owns a fixed device
+// memory pool and forbids allocation by libraries, an allocator-less embedded
+// runtime, or code that runs while another framework is capturing the stream
+// into a graph and allocation would break it.  They hand over every input and
+// output buffer themselves; the scratch the stage kernel needs (its run
+// descriptor, the binary at the stage time, per-tile ledger partials, block
+// counters, the max-speed word and the failure key) lives in the file-scope
+// array below, which every GPU that loads this library holds until the
+// process exits.
+constexpr size_t B2D_NOALLOC_SCRATCH_BYTES = 4u << 20;   // 4 MiB
+static __device__ __align__(256) unsigned char g_noalloc_scratch[B2D_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+constexpr int NOALLOC_MAX_DEVICES = 64;
+std::mutex g_noalloc_mutex;
+unsigned char* g_noalloc_base[NOALLOC_MAX_DEVICES] = {};
+}  // namespace
+
+// Device address of the scratch array on the current device.  The host-side
+// name g_noalloc_scratch is only a stand-in for the symbol, never a device
+// address: the address comes from cudaGetSymbolAddress, once per device.
+static b2d_status noalloc_scratch_base(unsigned char** base)
+{
+    int dev = 0;
+    CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return fail(B2D_ERR_INVALID, "device index out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_base[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p)
+            return fail(B2D_ERR_CUDA, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
+        g_noalloc_base[dev] = (unsigned char*)p;
+    }
+    *base = g_noalloc_base[dev];
+    return B2D_OK;
+}
+
+// The binary at the stage time, dt and the stage time, written into scratch.
+__global__ void noalloc_setup_kernel(RunDev* rd, double time, double dt)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        kepler_orbit(*rd, time, rd->orbit);
+        *rd->dt = dt;
+        rd->stage_time[0] = time;
+    }
+}
+
+extern "C" b2d_status b2d_stage_noalloc(const b2d_config* cfg, const double* d_in, const double* d_background,
+                                        const double* d_base, double* d_out, const double* d_ledger_in,
+                                        const double* d_ledger_base, double* d_ledger_out, double time, double dt,
+                                        double bf, double* d_max_speed, b2d_error* err_out, void* stream_ptr)
+{
+    if (!cfg || !d_in || !d_background || !d_out || !d_ledger_in || !d_ledger_out || (d_base && !d_ledger_base))
+        return fail(B2D_ERR_INVALID, "b2d_stage_noalloc: missing buffer");
+    b2d_status st = validate(*cfg, cfg->hydro_kind, cfg->rk_order);
+    if (st != B2D_OK) return st;
+    cudaStream_t stream = (cudaStream_t)stream_ptr;
+    const int nf = cfg->hydro_kind == B2D_EULER ? 4 : 3;
+    const int bs = cfg->block_size, nb = cfg->num_blocks, N = bs * nb, nblocks = nb * nb;
+    int tw = default_tile_w(bs), th = std::min(64, bs);
+    while (bs % th) th /= 2;
+    const int tiles_per_block = (bs / th) * (bs / tw);
+    const int ntiles = (N / th) * (N / tw);
+
+    // scratch layout: run descriptor | control words | counters | tile partials
+    const size_t off_run = 0, off_ctl = 2048, off_cnt = 2304;
+    const size_t off_part = off_cnt + ((sizeof(unsigned) * (size_t)nblocks + 255) / 256) * 256;
+    const size_t need = off_part + sizeof(double) * (size_t)nblocks * tiles_per_block * NITEMS * nf;
+    static_assert(sizeof(RunDev) <= 2048, "run descriptor outgrew its scratch slot");
+    if (need > B2D_NOALLOC_SCRATCH_BYTES)
+        return fail(B2D_ERR_INVALID, "b2d_stage_noalloc: this mesh needs " + std::to_string(need) +
+                                         " bytes of scratch; the library holds " +
+                                         std::to_string(B2D_NOALLOC_SCRATCH_BYTES) + " (use b2d_create instead)");
+    unsigned char* base = nullptr;
+    st = noalloc_scratch_base(&base);
+    if (st != B2D_OK) return st;
+
+    RunDev* d_run = (RunDev*)(base + off_run);
+    double* orbit = (double*)(base + off_ctl);            // 10 doubles
+    double* d_dt = orbit + 10;
+    double* stime = orbit + 11;
+    double* times = orbit + 12;                            // 4 doubles (unused by the stage)
+    long long* iters = (long long*)(orbit + 16);           // 4 (unused by the stage)
+    unsigned long long* amax = (unsigned long long*)(orbit + 20);
+    unsigned long long* err_key = amax + 1;
+    unsigned* timeout = (unsigned*)(err_key + 1);
+    unsigned* counter = (unsigned*)(base + off_cnt);
+    double* partial = (double*)(base + off_part);
+
+    std::vector<double> xc(N), xv((size_t)nb * (bs + 1));
+    for (int b = 0; b < nb; ++b) {
+        host_cell_centers(cfg, b, xc.data() + (size_t)b * bs);
+        host_block_vertices(cfg, b, xv.data() + (size_t)b * (bs + 1));
+    }
+    // the FP64 kernel reads its geometry from the run descriptor's tables: place
+    // them behind the partials in scratch
+    const size_t off_geo = ((need + 255) / 256) * 256;
+    const size_t need_geo = off_geo + sizeof(double) * (xc.size() + xv.size());
+    if (need_geo > B2D_NOALLOC_SCRATCH_BYTES)
+        return fail(B2D_ERR_INVALID, "b2d_stage_noalloc: mesh too large for the 4 MiB scratch (use b2d_create instead)");
+    double* d_xc = (double*)(base + off_geo);
+    double* d_xv = d_xc + xc.size();
+
+    RunDev rd;
+    memset(&rd, 0, sizeof rd);
+    rd.N = N; rd.bs = bs; rd.nb = nb; rd.nblocks = nblocks;
+    rd.tiles_i = N / th; rd.tiles_j = N / tw; rd.ntiles = ntiles; rd.tile_base = 0;
+    rd.tiles_per_block = tiles_per_block;
+    rd.xc = d_xc; rd.xv = d_xv;
+    rd.slot[0] = (void*)d_in; rd.slot[1] = (void*)d_base; rd.slot[2] = d_out; rd.slot[3] = d_out;
+    rd.bg = d_background;
+    rd.ledger[0] = (double*)d_ledger_in; rd.ledger[1] = (double*)d_ledger_base;
+    rd.ledger[2] = d_ledger_out; rd.ledger[3] = d_ledger_out;
+    rd.time = times; rd.iter = iters;
+    rd.partial = partial; rd.counter = counter;
+    rd.dt = d_dt; rd.stage_time = stime; rd.orbit = orbit; rd.amax = amax;
+    rd.binary_q = cfg->binary_mass_ratio; rd.binary_e = cfg->binary_eccentricity;
+    rd.p = make_params<double>(*cfg);
+    rd.pf = make_params<float>(*cfg);
+
+    // every call shares the scratch: reset what must start from zero (or ~0)
+    CUDA_TRY(cudaMemcpyAsync(d_run, &rd, sizeof rd, cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(cudaMemcpyAsync(d_xc, xc.data(), sizeof(double) * xc.size(), cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(cudaMemcpyAsync(d_xv, xv.data(), sizeof(double) * xv.size(), cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(unsigned) * nblocks, stream));
+    CUDA_TRY(cudaMemsetAsync(amax, 0, sizeof(unsigned long long), stream));
+    CUDA_TRY(cudaMemsetAsync(err_key, 0xff, sizeof(unsigned long long), stream));
+    CUDA_TRY(cudaMemsetAsync(timeout, 0, sizeof(unsigned), stream));
+    noalloc_setup_kernel<<<1, 32, 0, stream>>>(d_run, time, dt);
+    CUDA_TRY(cudaGetLastError());
+
+    StageArgs a;
+    a.runs = d_run;
+    a.nruns = 1;
+    a.th = th;
+    a.in_slot = 0;
+    a.base_slot = d_base ? 1 : -1;
+    a.out_slot = 2;
+    a.stage = 0;
+    a.amax_flag = d_max_speed ? 1 : 0;
+    a.bf = d_base ? bf : 0.0;
+    a.w1f = split_df(-a.bf + 1.0);
+    a.bff = split_df(a.bf);
+    a.err_key = err_key;
+    a.timeout_flag = timeout;
+    cudaError_t e = launch_stage_f64(nf, a, ntiles, tw, stage_smem_bytes(nf, 8, tw), stream);
+    if (e != cudaSuccess) return fail(B2D_ERR_CUDA, std::string("stage kernel launch: ") + cudaGetErrorString(e));
+    if (d_max_speed) CUDA_TRY(cudaMemcpyAsync(d_max_speed, amax, sizeof(double), cudaMemcpyDeviceToDevice, stream));
+
+    unsigned long long key = ~0ull;
+    CUDA_TRY(cudaMemcpyAsync(&key, err_key, sizeof key, cudaMemcpyDeviceToHost, stream));
+    CUDA_TRY(cudaStreamSynchronize(stream));
+    if (key == ~0ull) return B2D_OK;
+
+    // decode the failure key of the stage (see error_key in stage.cuh)
+    b2d_error err;
+    memset(&err, 0, sizeof err);
+    const int blk = (int)((key >> 30) & 0xffff), order = (int)((key >> 26) & 0xf);
+    const int zone = (int)((key >> 2) & 0xffffff);
+    err.code = (int)(key & 3);
+    err.block_i = (blk / nb + order / 3 - 1 + nb) % nb;
+    err.block_j = (blk % nb + order % 3 - 1 + nb) % nb;
+    err.zone_i = zone / bs;
+    err.zone_j = zone % bs;
+    const int gi = err.block_i * bs + err.zone_i, gj = err.block_j * bs + err.zone_j;
+    err.x = xc[gi];
+    err.y = xc[gj];
+    err.time = time;
+    double u[4] = {0, 0, 0, 0}, orb[10];
+    for (int f = 0; f < nf; ++f)
+        CUDA_TRY(cudaMemcpy(&u[f], d_in + (size_t)f * N * N + (size_t)gi * N + gj, sizeof(double),
+                            cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(orb, orbit, sizeof orb, cudaMemcpyDeviceToHost));
+    err.value = failure_value(*cfg, u, err.code);
+    err.binary[0] = orb[1]; err.binary[1] = orb[2]; err.binary[2] = orb[6]; err.binary[3] = orb[7];
+    if (err_out) *err_out = err;
+    return fail((b2d_status)err.code, "hydro error in b2d_stage_noalloc");
 }

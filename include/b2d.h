@@ -276,6 +276,38 @@ b2d_status b2d_unpin_host(void* ptr);
 /* Select the CUDA device used by contexts created afterwards on this thread. */
 b2d_status b2d_set_device(int32_t device);
 
+/* ------------------------------------------------------------------------ */
+/* One RK stage that allocates nothing.  No counterpart in the reference: it
+ * serves callers that cannot call cudaMalloc — a host code that owns a fixed
+ * device memory pool and forbids allocation by libraries, an allocator-less
+ * runtime, or code running while another framework captures the stream.
+ *
+ * Performs one try_advance_rk stage with the FP64 kernel on caller-owned
+ * device buffers: state planes [nf][N][N] (N = num_blocks · block_size,
+ * field-major, j contiguous) for the stage input, background, optional RK
+ * base (NULL: no averaging) and output; per-block ledgers
+ * [num_blocks][num_blocks][7][nf] in, base and out, with
+ *   out = (in + Σ sources · dx · dy) · (1 - bf) + base · bf   (base given)
+ *   out =  in + Σ sources · dx · dy                            (no base);
+ * `time` is the stage time, `dt` the step.  If d_max_speed is non-NULL the
+ * max signal speed of the output is written there (device double).
+ *
+ * Its scratch is one file-scope __device__ array of 4 MiB that every GPU that
+ * loads the library holds until exit; meshes whose tile partials and
+ * geometry tables do not fit are rejected with B2D_ERR_INVALID.  The first
+ * call on a device looks up the array's device address (cudaGetSymbolAddress)
+ * and should come before any stream capture.  All calls share the array:
+ * calls that overlap on the GPU (other streams, other host threads) race.
+ * The call synchronizes `stream` (a cudaStream_t, NULL for the default
+ * stream) to report hydro errors through err_out. */
+b2d_status b2d_stage_noalloc(const b2d_config* cfg, const double* d_in,
+                             const double* d_background, const double* d_base,
+                             double* d_out, const double* d_ledger_in,
+                             const double* d_ledger_base, double* d_ledger_out,
+                             double time, double dt, double bf,
+                             double* d_max_speed, b2d_error* err_out,
+                             void* stream);
+
 #ifdef __cplusplus
 }
 #endif
