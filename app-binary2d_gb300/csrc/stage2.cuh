@@ -25,20 +25,28 @@
 namespace b2d {
 
 constexpr int S2_DEPTH = 2;              // rows staged ahead of use
-constexpr int S2_SLOTS = S2_DEPTH + 4;   // a slot is read up to 3 rows after it lands
+constexpr int S2_SLOTS = S2_DEPTH + 4;   // stencil ring: a row is read again 3 rows after it lands
+constexpr int S2_USLOTS = S2_DEPTH + 1;  // update ring: a row is read once, at its update
 
-// Bytes of one staging slot (one tile row).
+// Bytes of one stencil slot: the stage input's stencil words of one tile row
+// with its halo (hi plane of the compensated store, or the FP64 state).
 __host__ __device__ inline int s2_slot_bytes(int nf, int store, int tw)
 {
-    if (store == 1) return 4 * (nf * (tw + 8) + 4 * nf * tw);   // hi (+halo) | lo | bg hi | base hi | base lo
-    return 8 * (nf * (tw + 4) + 2 * nf * tw);                   // state (+halo) | bg | base
+    return store == 1 ? 4 * nf * (tw + 8) : 8 * nf * (tw + 4);
+}
+
+// Bytes of one update slot: what the update of a row reads besides the stencil
+// words (compensated: lo | bg hi | base hi | base lo; FP64: bg | base).
+__host__ __device__ inline int s2_uslot_bytes(int nf, int store, int tw)
+{
+    return store == 1 ? 4 * 4 * nf * tw : 8 * 2 * nf * tw;
 }
 
 __host__ __device__ inline int s2_smem_bytes(int nf, int store, int tw)
 {
-    int slots = S2_SLOTS * s2_slot_bytes(nf, store, tw);
+    int slots = S2_SLOTS * s2_slot_bytes(nf, store, tw) + S2_USLOTS * s2_uslot_bytes(nf, store, tw);
     int exch = 16 * (2 * (tw + 4) + 3 * 2 * (tw + 2) + 2 * (tw + 1));
-    return slots + exch + 8 * S2_SLOTS;
+    return slots + exch + 8 * (S2_SLOTS + S2_USLOTS);
 }
 
 template <int NF>
@@ -101,8 +109,56 @@ template <int NF> __device__ __forceinline__ constexpr bool item_live(int k)
     return true;
 }
 
+template <int NF> __host__ __device__ constexpr int live_items()
+{
+    int n = 0;
+    for (int k = 0; k < NITEMS * NF; ++k) {
+        const int item = k / NF, f = k % NF;
+        bool dead = ((item == GRAV1 || item == GRAV2) && f == 0) || (NF == 3 && item == COOLING) ||
+                    (NF == 4 && item == FAKE_MASS);
+        n += dead ? 0 : 1;
+    }
+    return n;
+}
+
+template <int N> __host__ __device__ constexpr int pow2_at_least()
+{
+    int p = 1;
+    while (p < N) p <<= 1;
+    return p;
+}
+
+// Sum K values (K a power of two, K <= 32) over the 32 lanes of a warp by
+// recursive halving: after the call lane l holds the warp total of value
+// item_of_lane(l, K); 2K - 1 shuffles in all.
+template <int K> __device__ __forceinline__ float warp_sum_items(float (&v)[K], int lane)
+{
+#pragma unroll
+    for (int half = K / 2, off = 16; half >= 1; half >>= 1, off >>= 1) {
+        const bool upper = (lane & off) != 0;
+#pragma unroll
+        for (int i = 0; i < half; ++i) {
+            const float send = upper ? v[i] : v[i + half];
+            const float keep = upper ? v[i + half] : v[i];
+            v[i] = keep + __shfl_xor_sync(0xffffffffu, send, off);
+        }
+    }
+    float s = v[0];
+    for (int off = 16 / K; off >= 1; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+    return s;
+}
+
+// Which value of warp_sum_items lane l ends up holding.
+template <int K> __device__ __forceinline__ int item_of_lane(int lane)
+{
+    int item = 0;
+    for (int half = K / 2, off = 16; half >= 1; half >>= 1, off >>= 1)
+        if (lane & off) item += half;
+    return item;
+}
+
 template <int NF, int STORE>
-__global__ void __launch_bounds__(160) stage2_kernel(StageArgs a)
+__global__ void __launch_bounds__(160, (NF == 3 && STORE == 1) ? 4 : 3) stage2_kernel(StageArgs a)
 {
     using E = typename std::conditional<STORE == 1, float, double>::type;
     constexpr int H = STORE == 1 ? 4 : 2;     // staged halo columns per side: 16 bytes
@@ -159,13 +215,16 @@ __global__ void __launch_bounds__(160) stage2_kernel(StageArgs a)
     // ---- shared memory carve-up ------------------------------------------------
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const int SLOT = s2_slot_bytes(NF, STORE, TW);
-    unsigned char* slots = smem_raw;
-    float4* sP = (float4*)(slots + S2_SLOTS * SLOT);         // [2][TW+4]  primitives of a row
+    const int USLOT = s2_uslot_bytes(NF, STORE, TW);
+    unsigned char* slots = smem_raw;                          // stencil ring
+    unsigned char* uslots = slots + S2_SLOTS * SLOT;          // update ring
+    float4* sP = (float4*)(uslots + S2_USLOTS * USLOT);       // [2][TW+4]  primitives of a row
     float4* sR0 = sP + 2 * (TW + 4);                          // [2][TW+2]  cell record, 3 float4 planes
     float4* sR1 = sR0 + 2 * (TW + 2);
     float4* sR2 = sR1 + 2 * (TW + 2);
     float4* sF = sR2 + 2 * (TW + 2);                          // [2][TW+1]  y-face fluxes
-    uint64_t* bars = (uint64_t*)(sF + 2 * (TW + 1));
+    uint64_t* bars = (uint64_t*)(sF + 2 * (TW + 1));          // [S2_SLOTS] stencil ring
+    uint64_t* ubars = bars + S2_SLOTS;                        // [S2_USLOTS] update ring
 
     // ---- roles -----------------------------------------------------------------
     const bool interior = t < TW;
@@ -193,23 +252,28 @@ __global__ void __launch_bounds__(160) stage2_kernel(StageArgs a)
             bulk_load(dst + (H + TW) * sizeof(E), row + (j0 + TW) % N, H * sizeof(E), bar);
         }
     };
+    // stencil words of tile row r (r in [-2, TH+1]) into the stencil ring
     auto issue = [&](int r) {
         const int rr = r + 2;
         unsigned char* sb = slots + (rr % S2_SLOTS) * SLOT;
         uint64_t* bar = bars + rr % S2_SLOTS;
         const int gi = wrap(i0 + r, N);
-        const bool upd = r >= 0 && r < TH;
-        uint32_t bytes = NF * SW * sizeof(E);
-        if (upd) {
-            if (STORE == 1) bytes += (2 + (has_base ? 2 : 0)) * NF * TW * sizeof(E);
-            else bytes += (1 + (has_base ? 1 : 0)) * NF * TW * sizeof(E);
-        }
         fence_proxy_async();
-        mbar_arrive_expect_tx(bar, bytes);
+        mbar_arrive_expect_tx(bar, NF * SW * sizeof(E));
         const size_t roff = (size_t)gi * N;
         for (int f = 0; f < NF; ++f) copy_row(sb + f * SW * sizeof(E), plane(uin, f, 0) + roff, 1, bar);
-        if (upd) {
-            unsigned char* q = sb + NF * SW * sizeof(E);
+    };
+    // the rest of what the update of tile row r (r in [0, TH)) reads, into the update ring
+    auto issue_update = [&](int r) {
+        unsigned char* q = uslots + (r % S2_USLOTS) * USLOT;
+        uint64_t* bar = ubars + r % S2_USLOTS;
+        const size_t roff = (size_t)(i0 + r) * N;
+        uint32_t bytes;
+        if (STORE == 1) bytes = (2 + (has_base ? 2 : 0)) * NF * TW * sizeof(E);
+        else bytes = (1 + (has_base ? 1 : 0)) * NF * TW * sizeof(E);
+        fence_proxy_async();
+        mbar_arrive_expect_tx(bar, bytes);
+        {
             if (STORE == 1) {
                 for (int f = 0; f < NF; ++f, q += TW * sizeof(E)) copy_row(q, plane(uin, f, 1) + roff, 0, bar);
                 for (int f = 0; f < NF; ++f, q += TW * sizeof(E)) copy_row(q, plane(ubg, f, 0) + roff, 0, bar);
@@ -226,7 +290,7 @@ __global__ void __launch_bounds__(160) stage2_kernel(StageArgs a)
     };
 
     if (producer) {
-        for (int s = 0; s < S2_SLOTS; ++s) mbar_init(bars + s, 1);
+        for (int s = 0; s < S2_SLOTS + S2_USLOTS; ++s) mbar_init(bars + s, 1);
         fence_mbar_init();
     }
     __syncthreads();
@@ -247,9 +311,14 @@ __global__ void __launch_bounds__(160) stage2_kernel(StageArgs a)
     float Pm1[NF], P0[NF];               // primitives of rows rg-1, rg (own column)
     float rxa[2 * NF + 3], rxb[2 * NF + 3];  // x-face records of rows rq, rq+1: pc, gx, sxx, sxy, bulk
     float fxA[NF], fxB[NF];              // x fluxes at faces ru-1/2, ru+1/2
-    float led[NL];
-#pragma unroll
-    for (int k = 0; k < NL; ++k) led[k] = 0.0f;
+    // source ledger: per-warp accumulators of the live items, one lane each
+    constexpr int NLIVE = live_items<NF>();
+    constexpr int KL = pow2_at_least<NLIVE>();
+    __shared__ float sLed[4][32];
+    const int lane = t & 31, warp = t >> 5;
+    if (t < 128) sLed[t >> 5][t & 31] = 0.0f;
+    const int my_item = item_of_lane<KL>(lane);
+    const bool item_writer = my_item < NLIVE && (lane & (32 / KL - 1)) == 0;
     float amax = 0.0f;
 #pragma unroll
     for (int f = 0; f < NF; ++f) { Pm1[f] = P0[f] = fxA[f] = fxB[f] = 0.0f; }
@@ -258,7 +327,11 @@ __global__ void __launch_bounds__(160) stage2_kernel(StageArgs a)
 
     for (int k = 0; k < TH + 5; ++k) {
         const int rn = k - 2;
-        if (producer && rn + S2_DEPTH <= TH + 1) issue(rn + S2_DEPTH);
+        if (producer) {
+            if (rn + S2_DEPTH <= TH + 1) issue(rn + S2_DEPTH);
+            const int ur = rn - 3 + S2_DEPTH;                // update row needed S2_DEPTH rows from now
+            if (ur >= 0 && ur <= TH - 1) issue_update(ur);
+        }
 
         // ---- phase 1: row rn -> primitives (try_block_primitive, scheme.rs:185-199) --
         float pn[NF];
@@ -362,7 +435,8 @@ __global__ void __launch_bounds__(160) stage2_kernel(StageArgs a)
                 const float fyl[4] = {fl4.x, fl4.y, fl4.z, fl4.w}, fyr[4] = {fr4.x, fr4.y, fr4.z, fr4.w};
                 const float x = xc_row[rc];
                 float uc[NF], u0[NF];
-                const E* q = sb + NF * SW;
+                if (up_ok && !mbar_wait_bounded(ubars + rc % S2_USLOTS, (rc / S2_USLOTS) & 1)) timeout = 1;
+                const E* q = (const E*)(uslots + (rc % S2_USLOTS) * USLOT);
 #pragma unroll
                 for (int f = 0; f < NF; ++f) {
                     uc[f] = (float)sb[f * SW + c + H];
@@ -400,10 +474,17 @@ __global__ void __launch_bounds__(160) stage2_kernel(StageArgs a)
                         uc[f] = (float)o;
                     }
                 }
-                // a select, not a multiply by 0: the masked iterations may carry non-finite values
+                if (up_ok) {   // the same row for the whole warp
+                    float v[KL];
+                    int j = 0;
 #pragma unroll
-                for (int k2 = 0; k2 < NL; ++k2)
-                    if (item_live<NF>(k2)) led[k2] += up_ok ? it[k2] : 0.0f;
+                    for (int k2 = 0; k2 < NL; ++k2)
+                        if (item_live<NF>(k2)) v[j++] = it[k2];
+#pragma unroll
+                    for (int k2 = NLIVE; k2 < KL; ++k2) v[k2] = 0.0f;
+                    const float s = warp_sum_items<KL>(v, lane);
+                    if (item_writer) sLed[warp][my_item] += s;
+                }
                 if (want_amax && up_ok) amax = fmaxf(max_signal_speed<NF, float>(P, uc), amax);
             }
 
@@ -424,19 +505,18 @@ __global__ void __launch_bounds__(160) stage2_kernel(StageArgs a)
     // ---- per-tile ledger and max speed (deterministic tree over the CTA) -------------
     double* red = (double*)smem_raw;
     const int NT = blockDim.x;
-    for (int k = 0; k < NL; ++k) {
-        if (!item_live<NF>(k)) {
-            if (t == 0) rd.partial[((size_t)block * rd.tiles_per_block + tib) * NL + k] = 0.0;
-            continue;
+    if (t < NL) {
+        // live item index of ledger slot t, summed over the interior warps in order
+        int j = 0;
+        bool live = false;
+        for (int k2 = 0; k2 < NL; ++k2) {
+            if (k2 == t) { live = item_live<NF>(k2); break; }
+            if (item_live<NF>(k2)) ++j;
         }
-        red[t] = (double)led[k];
-        __syncthreads();
-        for (int s = 1; s < NT; s <<= 1) {
-            if ((t & (2 * s - 1)) == 0 && t + s < NT) red[t] += red[t + s];
-            __syncthreads();
-        }
-        if (t == 0) rd.partial[((size_t)block * rd.tiles_per_block + tib) * NL + k] = red[0];
-        __syncthreads();
+        double s = 0.0;
+        if (live)
+            for (int w = 0; w < TW / 32; ++w) s += (double)sLed[w][j];
+        rd.partial[((size_t)block * rd.tiles_per_block + tib) * NL + t] = s;
     }
     if (a.amax_flag) {
         red[t] = (double)amax;
