@@ -13,7 +13,9 @@ static cudaError_t launch_two(const StageArgs& a, int grid, int tw, cudaStream_t
     auto k = stage2_kernel<NF, STORE>;
     size_t smem = s2_smem_bytes(NF, STORE, tw);
     static size_t configured = 0;
-    if (smem > 48 * 1024 && smem > configured) {
+    // opt in for every size: the kernel's static shared memory counts toward
+    // the 48 KB that needs no opt-in
+    if (smem > configured) {
         cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         configured = smem;
