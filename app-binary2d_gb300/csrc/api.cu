@@ -743,6 +743,7 @@ static b2d_status launch_stage(b2d_ctx* ctx, const StagePlan& sp, int stage, int
     a.bff = split_df(sp.bf);
     a.err_key = ctx->d_err_key;
     a.timeout_flag = ctx->d_timeout;
+    a.pf1 = ctx->rdev_h[0].pf;
     size_t smem = stage_smem_bytes(ctx->nf, rsize_of(ctx->precision), ctx->tw);
     cudaError_t e;
     if (ctx->precision == B2D_PREC_FP64) e = launch_stage_f64(ctx->nf, a, ctx->total_tiles, ctx->tw, smem, ctx->stream);

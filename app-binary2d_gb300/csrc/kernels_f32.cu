@@ -7,10 +7,10 @@
 
 namespace b2d {
 
-template <int NF, int STORE>
-static cudaError_t launch_two(const StageArgs& a, int grid, int tw, cudaStream_t s)
+template <int NF, int STORE, bool SINGLE>
+static cudaError_t launch_two_impl(const StageArgs& a, int grid, int tw, cudaStream_t s)
 {
-    auto k = stage2_kernel<NF, STORE>;
+    auto k = stage2_kernel<NF, STORE, SINGLE>;
     size_t smem = s2_smem_bytes(NF, STORE, tw);
     static size_t configured = 0;
     // opt in for every size: the kernel's static shared memory counts toward
@@ -22,6 +22,13 @@ static cudaError_t launch_two(const StageArgs& a, int grid, int tw, cudaStream_t
     }
     k<<<grid, tw + 32, smem, s>>>(a);
     return cudaGetLastError();
+}
+
+template <int NF, int STORE>
+static cudaError_t launch_two(const StageArgs& a, int grid, int tw, cudaStream_t s)
+{
+    if (a.nruns == 1) return launch_two_impl<NF, STORE, true>(a, grid, tw, s);
+    return launch_two_impl<NF, STORE, false>(a, grid, tw, s);
 }
 
 cudaError_t launch_stage_f32(int nf, int store, const StageArgs& a, int grid, int tw, size_t smem, cudaStream_t s)

@@ -44,6 +44,7 @@ struct StageArgs {
     int amax_flag;
     double bf;               // weight of the RK base state (br of godunov-core)
     b2d::df32w w1f, bff;     // 1 - bf and bf as double-float
+    DevParamsF pf1;          // FP32 parameters of a single-run context, read as kernel arguments
     unsigned long long* err_key;  // failure key, ~0 when no zone failed
     unsigned* timeout_flag;       // set when a bounded wait gave up
 };

@@ -157,7 +157,14 @@ template <int K> __device__ __forceinline__ int item_of_lane(int lane)
     return item;
 }
 
-template <int NF, int STORE>
+template <bool SINGLE>
+__device__ __forceinline__ const DevParamsF& params_for(const StageArgs& a, const DevParamsF& shared_copy)
+{
+    if constexpr (SINGLE) return a.pf1;
+    else return shared_copy;
+}
+
+template <int NF, int STORE, bool SINGLE>
 __global__ void __launch_bounds__(160, (NF == 3 && STORE == 1) ? 4 : 3) stage2_kernel(StageArgs a)
 {
     using E = typename std::conditional<STORE == 1, float, double>::type;
@@ -175,7 +182,11 @@ __global__ void __launch_bounds__(160, (NF == 3 && STORE == 1) ? 4 : 3) stage2_k
     const RunDev& rd = a.runs[ri];
     if (g - rd.tile_base >= rd.ntiles) return;
 
-    __shared__ DevParamsF P;
+    // Physics parameters: a single-run launch reads them from the kernel
+    // arguments (constant-bank operands, no load instruction); a batched
+    // launch stages its run's parameters in shared memory.
+    __shared__ DevParamsF Psh;
+    const DevParamsF& P = params_for<SINGLE>(a, Psh);
     __shared__ Binary<float> B;
     __shared__ double orbd[10];
     __shared__ int failed, timeout;
@@ -185,7 +196,7 @@ __global__ void __launch_bounds__(160, (NF == 3 && STORE == 1) ? 4 : 3) stage2_k
     }
     __syncthreads();
     if (failed) return;
-    if (t == 0) P = rd.pf;
+    if (!SINGLE && t == 0) Psh = rd.pf;
     if (t < 10) orbd[t] = rd.orbit[a.stage * 10 + t];
     __syncthreads();
     if (t == 0) {
@@ -424,7 +435,7 @@ __global__ void __launch_bounds__(160, (NF == 3 && STORE == 1) ? 4 : 3) stage2_k
             if (fy_ok) sF[(rq & 1) * (TW + 1) + c] = make_float4(F[0], F[1], F[2], NF == 4 ? F[NF - 1] : 0.0f);
         };
         float fxn[NF];
-        if (interior) {
+        if (interior && rn >= 1) {   // before rn = 1 no face or update row is valid
             y_flux();
 
             // update of row ru
