@@ -76,6 +76,15 @@ def sweep(nruns: int = 64, seed: int = 4):
     return out
 
 
+def annulus_tracers(n: int, seed: int = 5, r_in: float = 1.0, r_out: float = 6.0):
+    """n tracer positions uniform in area over the annulus r_in < r < r_out."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    r = np.sqrt(rng.uniform(r_in * r_in, r_out * r_out, n))
+    phi = rng.uniform(0.0, 2.0 * np.pi, n)
+    return np.stack([r * np.cos(phi), r * np.sin(phi)], axis=1)
+
+
 def disk_8192(seed: int = 5):
     """Single large isothermal run, q = 1, e = 0.1, 64×64 blocks of 128²."""
     return iso_disk(64, 128, seed=seed, e=0.1)

@@ -148,6 +148,20 @@ class Runtime:
         _check(self.lib.b2d_download_ledger(self.ctx, run, _dp(out)))
         return out
 
+    def set_tracers(self, run: int, xy: np.ndarray):
+        """Massless tracers of a run: `xy` of shape [n, 2]."""
+        xy = np.ascontiguousarray(xy, dtype=np.float64).reshape(-1, 2)
+        self._ntracers = getattr(self, "_ntracers", {})
+        self._ntracers[run] = len(xy)
+        _check(self.lib.b2d_set_tracers(self.ctx, run, len(xy), _dp(xy) if len(xy) else None))
+
+    def tracers(self, run: int = 0) -> np.ndarray:
+        n = getattr(self, "_ntracers", {}).get(run, 0)
+        out = np.empty((n, 2), dtype=np.float64)
+        if n:
+            _check(self.lib.b2d_get_tracers(self.ctx, run, _dp(out)))
+        return out
+
     def max_signal_speed(self, run: int = 0) -> float:
         v = ctypes.c_double(0)
         _check(self.lib.b2d_max_signal_speed(self.ctx, run, ctypes.byref(v)))

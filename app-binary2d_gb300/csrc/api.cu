@@ -379,6 +379,9 @@ static void free_ctx(b2d_ctx* ctx)
     for (auto& kv : ctx->graphs) cudaGraphExecDestroy(kv.second);
     for (RunHost& r : ctx->runs) {
         for (int s = 0; s < NSLOTS; ++s) { cudaFree(r.slot[s]); cudaFree(r.ledger[s]); }
+        const size_t ri = &r - ctx->runs.data();
+        if (ri < ctx->rdev_h.size())
+            for (int s = 0; s < NSLOTS; ++s) cudaFree(ctx->rdev_h[ri].tracers[s]);
         cudaFree(r.bg); cudaFree(r.partial); cudaFree(r.counter);
         cudaFree(r.xc); cudaFree(r.xv); cudaFree(r.xcf); cudaFree(r.xvf);
         cudaFree(r.stage_time); cudaFree(r.orbit);
@@ -752,6 +755,88 @@ static b2d_status launch_stage(b2d_ctx* ctx, const StagePlan& sp, int stage, int
     return B2D_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Massless tracer particles (no counterpart in the reference's code; its
+// README names them).  dx/dt = v(x, t) with v the gas velocity of the stage
+// input, bilinear between the four surrounding cell centres of the uniform
+// mesh, advanced by the same RK stages and weighted averages as the state and
+// wrapped into the periodic domain [-R, R)^2.  Positions are FP64.
+template <int NF, int STORE>
+__device__ __forceinline__ void tracer_cell_velocity(const RunDev& rd, int slot, int i, int j, double& vx, double& vy)
+{
+    const size_t nn = (size_t)rd.N * rd.N, idx = (size_t)i * rd.N + j;
+    double u[3];
+    for (int f = 0; f < 3; ++f) {
+        if (STORE == 0) u[f] = ((const double*)rd.slot[slot])[f * nn + idx];
+        else {
+            const float* p = (const float*)rd.slot[slot];
+            u[f] = (double)p[(2 * f) * nn + idx] + (double)p[(2 * f + 1) * nn + idx];
+        }
+    }
+    vx = u[1] / u[0];
+    vy = u[2] / u[0];
+}
+
+template <int NF, int STORE>
+__global__ void tracer_kernel(const RunDev* runs, int run, int in_slot, int base_slot, int out_slot, double bf)
+{
+    const RunDev& rd = runs[run];
+    const long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (k >= rd.ntracers) return;
+    const double R = rd.p.domain_radius, dx = rd.p.dx, dt = *rd.dt;
+    const int N = rd.N;
+    const double x = rd.tracers[in_slot][2 * k], y = rd.tracers[in_slot][2 * k + 1];
+    const double gx = (x + R) / dx - 0.5, gy = (y + R) / dx - 0.5;
+    const double fi = floor(gx), fj = floor(gy);
+    const double ax = gx - fi, ay = gy - fj;
+    int i0 = (int)fi, j0 = (int)fj;
+    i0 = ((i0 % N) + N) % N;
+    j0 = ((j0 % N) + N) % N;
+    const int i1 = i0 + 1 == N ? 0 : i0 + 1, j1 = j0 + 1 == N ? 0 : j0 + 1;
+    double v00x, v00y, v10x, v10y, v01x, v01y, v11x, v11y;
+    tracer_cell_velocity<NF, STORE>(rd, in_slot, i0, j0, v00x, v00y);
+    tracer_cell_velocity<NF, STORE>(rd, in_slot, i1, j0, v10x, v10y);
+    tracer_cell_velocity<NF, STORE>(rd, in_slot, i0, j1, v01x, v01y);
+    tracer_cell_velocity<NF, STORE>(rd, in_slot, i1, j1, v11x, v11y);
+    const double w00 = (1.0 - ax) * (1.0 - ay), w10 = ax * (1.0 - ay), w01 = (1.0 - ax) * ay, w11 = ax * ay;
+    const double vx = w00 * v00x + w10 * v10x + w01 * v01x + w11 * v11x;
+    const double vy = w00 * v00y + w10 * v10y + w01 * v01y + w11 * v11y;
+    double xo = x + dt * vx, yo = y + dt * vy;
+    const double L = 2.0 * R;
+    if (base_slot >= 0) {
+        // average with the base position on the same periodic image
+        const double xb = rd.tracers[base_slot][2 * k], yb = rd.tracers[base_slot][2 * k + 1];
+        if (xo - xb > R) xo -= L;
+        else if (xo - xb < -R) xo += L;
+        if (yo - yb > R) yo -= L;
+        else if (yo - yb < -R) yo += L;
+        xo = xo * (-bf + 1.0) + xb * bf;
+        yo = yo * (-bf + 1.0) + yb * bf;
+    }
+    if (xo >= R) xo -= L;
+    if (xo < -R) xo += L;
+    if (yo >= R) yo -= L;
+    if (yo < -R) yo += L;
+    rd.tracers[out_slot][2 * k] = xo;
+    rd.tracers[out_slot][2 * k + 1] = yo;
+}
+
+static b2d_status launch_tracers(b2d_ctx* ctx, const StagePlan& sp, bool count)
+{
+    for (int r = 0; r < ctx->nruns; ++r) {
+        const long long n = ctx->rdev_h[r].ntracers;
+        if (n <= 0) continue;
+        const int threads = 256;
+        const unsigned grid = (unsigned)((n + threads - 1) / threads);
+        const int store = ctx->precision == B2D_PREC_FP32_COMP ? 1 : 0;
+        if (store == 0) tracer_kernel<3, 0><<<grid, threads, 0, ctx->stream>>>(ctx->rdev, r, sp.in, sp.base, sp.out, sp.bf);
+        else tracer_kernel<3, 1><<<grid, threads, 0, ctx->stream>>>(ctx->rdev, r, sp.in, sp.base, sp.out, sp.bf);
+        CUDA_TRY(cudaGetLastError());
+        if (count) ctx->launches++;
+    }
+    return B2D_OK;
+}
+
 static b2d_status enqueue_advance(b2d_ctx* ctx, int fold, int start, int* final_slot, bool count)
 {
     std::vector<StagePlan> plan = plan_advance(ctx->rk, fold, start, final_slot);
@@ -773,7 +858,41 @@ static b2d_status enqueue_advance(b2d_ctx* ctx, int fold, int start, int* final_
         if (st != B2D_OK) return st;
         if (timed) CUDA_TRY(cudaEventRecord(ctx->ev[2 * s + 1], ctx->stream));
         if (count) ctx->launches++;
+        st = launch_tracers(ctx, plan[s], count);
+        if (st != B2D_OK) return st;
     }
+    return B2D_OK;
+}
+
+extern "C" b2d_status b2d_set_tracers(b2d_ctx* ctx, int32_t run, int64_t n, const double* xy)
+{
+    if (!ctx || run < 0 || run >= ctx->nruns || n < 0 || (n > 0 && !xy)) return fail(B2D_ERR_INVALID, "bad arguments");
+    CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    RunDev& d = ctx->rdev_h[run];
+    for (int s = 0; s < NSLOTS; ++s) {
+        CUDA_TRY(cudaFree(d.tracers[s]));
+        d.tracers[s] = nullptr;
+    }
+    d.ntracers = 0;
+    if (n > 0) {
+        for (int s = 0; s < NSLOTS; ++s) CUDA_TRY(cudaMalloc(&d.tracers[s], sizeof(double) * 2 * (size_t)n));
+        CUDA_TRY(cudaMemcpy(d.tracers[ctx->cur], xy, sizeof(double) * 2 * (size_t)n, cudaMemcpyHostToDevice));
+        d.ntracers = n;
+    }
+    CUDA_TRY(cudaMemcpy(ctx->rdev, ctx->rdev_h.data(), sizeof(RunDev) * ctx->nruns, cudaMemcpyHostToDevice));
+    for (auto& kv : ctx->graphs) cudaGraphExecDestroy(kv.second);
+    ctx->graphs.clear();
+    return B2D_OK;
+}
+
+extern "C" b2d_status b2d_get_tracers(b2d_ctx* ctx, int32_t run, double* xy)
+{
+    if (!ctx || run < 0 || run >= ctx->nruns || !xy) return fail(B2D_ERR_INVALID, "bad arguments");
+    const RunDev& d = ctx->rdev_h[run];
+    if (d.ntracers > 0)
+        CUDA_TRY(cudaMemcpyAsync(xy, d.tracers[ctx->cur], sizeof(double) * 2 * (size_t)d.ntracers,
+                                 cudaMemcpyDeviceToHost, ctx->stream));
+    CUDA_TRY(cudaStreamSynchronize(ctx->stream));
     return B2D_OK;
 }
 
@@ -818,7 +937,7 @@ static b2d_status run_advance(b2d_ctx* ctx, int fold, int* final_slot)
         plan_advance(ctx->rk, fold, start, final_slot);
     }
     CUDA_TRY(cudaGraphLaunch(it->second, ctx->stream));
-    ctx->launches += 1 + (long long)fold * ctx->rk;
+    ctx->launches += b2d_launches_per_advance(ctx, fold);
     return B2D_OK;
 }
 
@@ -978,7 +1097,10 @@ extern "C" int64_t b2d_launch_count(const b2d_ctx* ctx) { return ctx ? ctx->laun
 
 extern "C" int64_t b2d_launches_per_advance(const b2d_ctx* ctx, int32_t fold)
 {
-    return ctx ? 1 + (int64_t)fold * ctx->rk : 0;
+    if (!ctx) return 0;
+    int with_tracers = 0;
+    for (const RunDev& d : ctx->rdev_h) with_tracers += d.ntracers > 0 ? 1 : 0;
+    return 1 + (int64_t)fold * ctx->rk * (1 + with_tracers);
 }
 
 extern "C" b2d_status b2d_set_instrument(b2d_ctx* ctx, int32_t enable)

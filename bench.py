@@ -201,18 +201,30 @@ def ours(args):
     elif args.workload == "disk_1024":
         mesh, hydro, physics, model = b2.presets.iso_disk(8, 128, seed=1 + rank)
         wname = "iso disk 1024^2 (8x8 blocks of 128^2)"
+    elif args.workload == "euler_4096":
+        mesh, hydro, physics, model = b2.presets.euler_beta_disk(seed=3 + rank)
+        wname = ("Euler disk 4096^2 (32x32 blocks of 128^2), gamma 5/3, beta-cooling 10, alpha 0.1, "
+                 "q=0.5 e=0.5, RK2, fold 10")
+    elif args.workload == "disk_8192":
+        mesh, hydro, physics, model = b2.presets.disk_8192(seed=5 + rank)
+        wname = "iso disk 8192^2 (64x64 blocks of 128^2), q=1 e=0.1, RK2, fold 10"
+        if args.tracers < 0:
+            args.tracers = 10_000_000
     else:
         raise SystemExit("unknown workload")
-    nf = 3
+    nf = b2.num_fields(hydro)
     zones = mesh.total_zones()
     cons = b2.initial_state(mesh, hydro, physics, model)
     run = b2.Run(mesh, hydro, physics)
+    tracers = b2.presets.annulus_tracers(args.tracers, seed=5 + rank) if args.tracers > 0 else None
 
     tuned = {}
 
     def make(prec):
         rt = b2.Runtime([run], precision=prec)
         rt.upload(0, cons)
+        if tracers is not None:
+            rt.set_tracers(0, tracers)
         if args.tile:
             rt.set_tile(*[int(x) for x in args.tile.split("x")])
         elif prec in tuned:
@@ -253,7 +265,9 @@ def ours(args):
 
     prec = args.precision
     w = 8  # stored bytes per conserved word (FP64, or FP32 + FP32 compensation)
-    bytes_per_zone_update = 7 * nf * w          # RK2: 3 reads + 1 write, 2 reads + 1 write ... see the design doc
+    # RK2: stage 1 reads U and U_bg and writes U1; stage 2 reads U1, U and U_bg and
+    # writes U2: 7 accesses of nf words of w bytes per zone-update
+    bytes_per_zone_update = 7 * nf * w
     hbm_peak, peak_kind = peaks()
 
     rt = make(prec)
@@ -329,6 +343,8 @@ def ours(args):
                                                              "fp32_comp": "f32 (compensated f32 state)"}[prec],
             "data": "synthetic",
             "config": {"workload": wname, "precision": prec, "zones": zones, "fold": FOLD,
+                       "tracers": int(args.tracers) if tracers is not None else 0,
+                       "tracer_bytes_per_step": (2 * 32 * FOLD * int(args.tracers)) if tracers is not None else 0,
                        "global_batch": ws, "parallelism": "replicas" if ws > 1 else "single GPU",
                        "l2": "state + background > L2 (no flush needed)",
                        "tile": "%dx%d" % tuned.get(prec, (0, 0)) if not args.tile else args.tile,
@@ -494,6 +510,7 @@ def main():
     ap.add_argument("--workload", default="disk_2048")
     ap.add_argument("--tile", default="")
     ap.add_argument("--sweep-runs", type=int, default=64)
+    ap.add_argument("--tracers", type=int, default=-1, help="tracer particles (-1: workload default)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--accuracy-orbits", type=float, default=1.0)
     ap.add_argument("--skip-cpu", action="store_true")

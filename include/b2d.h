@@ -203,6 +203,14 @@ b2d_status b2d_advance(b2d_ctx* ctx, int32_t fold, double* dt_out,
 b2d_status b2d_advance_async(b2d_ctx* ctx, int32_t fold);
 b2d_status b2d_synchronize(b2d_ctx* ctx, double* dt_out, b2d_error* err_out);
 
+/* Massless tracer particles of one run (no counterpart in the reference's
+ * code; its README names them).  `xy` holds n (x, y) pairs.  Each RK stage
+ * moves a tracer with the stage input's gas velocity, bilinearly interpolated
+ * between the four surrounding cell centres, with the same weighted averages
+ * as the state, and wraps it into the periodic domain.  n = 0 removes them. */
+b2d_status b2d_set_tracers(b2d_ctx* ctx, int32_t run, int64_t n, const double* xy);
+b2d_status b2d_get_tracers(b2d_ctx* ctx, int32_t run, double* xy);
+
 /* State::max_signal_speed (src/state.rs:121-133) of one run. */
 b2d_status b2d_max_signal_speed(b2d_ctx* ctx, int32_t run, double* out);
 

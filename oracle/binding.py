@@ -39,7 +39,7 @@ def load():
         vp = ctypes.c_void_p
         lib.oracle_advance.restype = c_int32
         lib.oracle_advance.argtypes = [vp, c_dp, c_dp, c_dp, c_dp, ctypes.POINTER(ctypes.c_int64), c_int32, c_dp,
-                                       c_int32, ctypes.POINTER(OracleError)]
+                                       c_int32, ctypes.POINTER(OracleError), c_dp, ctypes.c_int64]
         lib.oracle_max_signal_speed.restype = c_double
         lib.oracle_max_signal_speed.argtypes = [vp, c_dp]
         lib.oracle_initial_state.restype = c_int32
@@ -89,6 +89,10 @@ class OracleState:
         self.ledger = np.zeros((nb, nb, 7, nf)) if ledger is None else np.array(ledger, dtype=np.float64)
         self.time = ctypes.c_double(time)
         self.iteration = ctypes.c_int64(iteration)
+        self.tracers = None
+
+    def set_tracers(self, xy):
+        self.tracers = np.array(xy, dtype=np.float64).reshape(-1, 2).copy()
 
     def advance(self, fold, nthreads=None):
         lib = load()
@@ -96,9 +100,11 @@ class OracleState:
             nthreads = 2 * (os.cpu_count() or 1)
         dt = ctypes.c_double(0)
         err = OracleError()
+        tr = self.tracers
         rc = lib.oracle_advance(ctypes.byref(self.cfg), _dp(self.cons), _dp(self.ledger), _dp(self.background),
                                 ctypes.byref(self.time), ctypes.byref(self.iteration), int(fold), ctypes.byref(dt),
-                                int(nthreads), ctypes.byref(err))
+                                int(nthreads), ctypes.byref(err), None if tr is None else _dp(tr),
+                                0 if tr is None else len(tr))
         if rc:
             raise OracleHydroError(err)
         return dt.value

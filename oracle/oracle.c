@@ -787,9 +787,64 @@ static void task_update(pool* pl, int w, int b)
 typedef struct rk_state {
     double* cons;
     double* led;
+    double* tr;       /* tracer positions [n][2] */
     double time;
     int64_t iteration;
 } rk_state;
+
+/* Massless tracers (no reference code: its README names them).  dx/dt =
+ * v(x) with v the stage input's gas velocity, bilinear between the four
+ * surrounding cell centres of the uniform mesh; the stage's weighted average
+ * with the base position is taken on the same periodic image; positions wrap
+ * into [-R, R). */
+static void tracer_velocity(const stage_ctx* s, const double* cons, int i, int j, double* vx, double* vy)
+{
+    int bs = s->bs, nb = s->nb, nf = s->nf;
+    const double* u = cons + ((((size_t)(i / bs) * nb + j / bs) * bs + i % bs) * bs + j % bs) * nf;
+    *vx = u[1] / u[0];
+    *vy = u[2] / u[0];
+}
+
+static void advance_tracers(const stage_ctx* s, const double* cons_in, const double* tin, const double* tbase,
+                            double bf, double* tout, int64_t n)
+{
+    const double R = s->c->domain_radius, dx = s->dx, dt = s->dt, L = 2.0 * R;
+    const int N = s->nb * s->bs;
+    for (int64_t k = 0; k < n; ++k) {
+        double x = tin[2 * k], y = tin[2 * k + 1];
+        double gx = (x + R) / dx - 0.5, gy = (y + R) / dx - 0.5;
+        double fi = floor(gx), fj = floor(gy);
+        double ax = gx - fi, ay = gy - fj;
+        int i0 = (int)fi, j0 = (int)fj;
+        i0 = ((i0 % N) + N) % N;
+        j0 = ((j0 % N) + N) % N;
+        int i1 = i0 + 1 == N ? 0 : i0 + 1, j1 = j0 + 1 == N ? 0 : j0 + 1;
+        double v00x, v00y, v10x, v10y, v01x, v01y, v11x, v11y;
+        tracer_velocity(s, cons_in, i0, j0, &v00x, &v00y);
+        tracer_velocity(s, cons_in, i1, j0, &v10x, &v10y);
+        tracer_velocity(s, cons_in, i0, j1, &v01x, &v01y);
+        tracer_velocity(s, cons_in, i1, j1, &v11x, &v11y);
+        double w00 = (1.0 - ax) * (1.0 - ay), w10 = ax * (1.0 - ay), w01 = (1.0 - ax) * ay, w11 = ax * ay;
+        double vx = w00 * v00x + w10 * v10x + w01 * v01x + w11 * v11x;
+        double vy = w00 * v00y + w10 * v10y + w01 * v01y + w11 * v11y;
+        double xo = x + dt * vx, yo = y + dt * vy;
+        if (tbase) {
+            double xb = tbase[2 * k], yb = tbase[2 * k + 1];
+            if (xo - xb > R) xo -= L;
+            else if (xo - xb < -R) xo += L;
+            if (yo - yb > R) yo -= L;
+            else if (yo - yb < -R) yo += L;
+            xo = xo * (-bf + 1.0) + xb * bf;
+            yo = yo * (-bf + 1.0) + yb * bf;
+        }
+        if (xo >= R) xo -= L;
+        if (xo < -R) xo += L;
+        if (yo >= R) yo -= L;
+        if (yo < -R) yo += L;
+        tout[2 * k] = xo;
+        tout[2 * k + 1] = yo;
+    }
+}
 
 static void weighted_average(rk_state* s1, double bf, const rk_state* s0, size_t ncons,
                              size_t nled)
@@ -805,10 +860,13 @@ typedef struct advance_ctx {
     pool* pl;
     int failed;
     oracle_error err;
+    int64_t ntracers;
 } advance_ctx;
 
-/* One call of try_advance_rk: state `in` -> `out` at time in->time. */
-static int stage(advance_ctx* a, const rk_state* in, rk_state* out)
+/* One call of try_advance_rk: state `in` -> `out` at time in->time.  Tracers
+ * are advanced here too; `base`/`bf` give the weighted average that follows
+ * the stage (NULL: none). */
+static int stage(advance_ctx* a, const rk_state* in, rk_state* out, const rk_state* base, double bf)
 {
     stage_ctx* s = &a->st;
     s->time = in->time;
@@ -853,6 +911,8 @@ static int stage(advance_ctx* a, const rk_state* in, rk_state* out)
     }
     pool_run(a->pl, nblocks, task_fluxes);
     pool_run(a->pl, nblocks, task_update);
+    if (a->ntracers > 0)
+        advance_tracers(s, in->cons, in->tr, base ? base->tr : NULL, bf, out->tr, a->ntracers);
     out->time = in->time + s->dt;
     out->iteration = in->iteration + 1;
     return 0;
@@ -869,7 +929,7 @@ double oracle_max_signal_speed(const oracle_config* c, const double* cons)
 
 int oracle_advance(const oracle_config* c, double* cons, double* ledger, const double* background,
                    double* time, int64_t* iteration, int32_t fold, double* dt_out,
-                   int32_t nthreads, oracle_error* err)
+                   int32_t nthreads, oracle_error* err, double* tracers, int64_t ntracers)
 {
     int nf = nfields(c), nb = c->num_blocks, bs = c->block_size;
     int nblocks = nb * nb;
@@ -912,10 +972,13 @@ int oracle_advance(const oracle_config* c, double* cons, double* ledger, const d
 
     /* five state slots: s0 (input), s1, s2, s3 and a spare */
     rk_state st[4];
+    a.ntracers = tracers ? ntracers : 0;
     for (int k = 0; k < 4; ++k) {
         st[k].cons = malloc(sizeof(double) * ncons);
         st[k].led = calloc(nled, sizeof(double));
+        st[k].tr = a.ntracers > 0 ? malloc(sizeof(double) * 2 * (size_t)a.ntracers) : NULL;
     }
+    if (a.ntracers > 0) memcpy(st[0].tr, tracers, sizeof(double) * 2 * (size_t)a.ntracers);
     memcpy(st[0].cons, cons, sizeof(double) * ncons);
     if (ledger) memcpy(st[0].led, ledger, sizeof(double) * nled);
     st[0].time = *time;
@@ -942,22 +1005,22 @@ int oracle_advance(const oracle_config* c, double* cons, double* ledger, const d
     for (int f = 0; f < fold && !rc; ++f) {
         rk_state* s0 = &st[0];
         if (c->rk_order == 1) {
-            rc = stage(&a, s0, &st[1]);
+            rc = stage(&a, s0, &st[1], NULL, 0.0);
             if (!rc) { rk_state t = st[0]; st[0] = st[1]; st[1] = t; }
         } else if (c->rk_order == 2) {
-            rc = stage(&a, s0, &st[1]);
-            if (!rc) rc = stage(&a, &st[1], &st[2]);
+            rc = stage(&a, s0, &st[1], NULL, 0.0);
+            if (!rc) rc = stage(&a, &st[1], &st[2], s0, 0.5);
             if (!rc) {
                 weighted_average(&st[2], 0.5, s0, ncons, nled);      /* br = 1/2 */
                 st[2].iteration = (st[2].iteration + s0->iteration) / 2;
                 rk_state t = st[0]; st[0] = st[2]; st[2] = t;
             }
         } else {
-            rc = stage(&a, s0, &st[1]);
-            if (!rc) rc = stage(&a, &st[1], &st[2]);
+            rc = stage(&a, s0, &st[1], NULL, 0.0);
+            if (!rc) rc = stage(&a, &st[1], &st[2], s0, 3.0 / 4.0);
             if (!rc) {
                 weighted_average(&st[2], 3.0 / 4.0, s0, ncons, nled); /* br = 3/4 */
-                rc = stage(&a, &st[2], &st[3]);
+                rc = stage(&a, &st[2], &st[3], s0, 1.0 / 3.0);
             }
             if (!rc) {
                 weighted_average(&st[3], 1.0 / 3.0, s0, ncons, nled); /* br = 1/3 */
@@ -981,11 +1044,12 @@ int oracle_advance(const oracle_config* c, double* cons, double* ledger, const d
         if (ledger) memcpy(ledger, st[0].led, sizeof(double) * nled);
         *time = st[0].time;
         *iteration = st[0].iteration;
+        if (a.ntracers > 0) memcpy(tracers, st[0].tr, sizeof(double) * 2 * (size_t)a.ntracers);
     } else if (err) {
         *err = a.err;
     }
 
-    for (int k = 0; k < 4; ++k) { free(st[k].cons); free(st[k].led); }
+    for (int k = 0; k < 4; ++k) { free(st[k].cons); free(st[k].led); free(st[k].tr); }
     for (int t = 0; t < nthreads; ++t) free(s->scratch[t]);
     free(s->scratch);
     free(s->xc); free(s->xv); free(s->prim); free(s->perr); free(s->pbad); free(s->pzone);

@@ -101,7 +101,8 @@ typedef struct oracle_point_mass { double m, x, y, vx, vy; } oracle_point_mass;
 int oracle_advance(const oracle_config* cfg, double* cons, double* ledger,
                    const double* background, double* time, int64_t* iteration,
                    int32_t fold, double* dt_out, int32_t nthreads,
-                   oracle_error* err);
+                   oracle_error* err, double* tracers /* [n][2] or NULL */,
+                   int64_t ntracers);
 
 double oracle_max_signal_speed(const oracle_config* cfg, const double* cons);
 

@@ -79,7 +79,7 @@ def test_initial_state_noise_is_layout_independent():
 
 
 # ----------------------------------------------------------------------------
-# oracle identities (SURVEY-style self-consistency checks)
+# oracle identities (self-consistency checks of the restatement)
 
 
 def test_plm_gradient_properties(oracle_lib):
