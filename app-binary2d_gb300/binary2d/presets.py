@@ -50,7 +50,10 @@ def euler_beta_disk(num_blocks: int = 32, block_size: int = 128, seed: int = 3):
     """Euler disk with β-cooling (β = 10), α-viscosity 0.1, q = 0.5, e = 0.5,
     γ = 5/3, model Mach 10 (4096² by default)."""
     mesh = Mesh(num_blocks=num_blocks, block_size=block_size, domain_radius=8.0)
-    hydro = Euler(gamma_law_index=5.0 / 3.0, cooling_coefficient=0.0, cooling_beta=10.0)
+    # the cold gas falling onto the binary needs the reference's floors
+    # (physics.rs:631-660) to keep the conversion to primitives defined
+    hydro = Euler(gamma_law_index=5.0 / 3.0, cooling_coefficient=0.0, cooling_beta=10.0,
+                  pressure_floor=1e-8, density_floor=1e-6)
     physics = Physics(buffer_rate=1000.0, buffer_scale=0.3, binary_eccentricity=0.5, binary_mass_ratio=0.5,
                       cfl=0.4, plm=1.5, rk_order="RK2", sink_radius=0.05, sink_rate=10.0,
                       viscosity=("alpha", 0.1), softening_length=0.05)
@@ -76,13 +79,22 @@ def sweep(nruns: int = 64, seed: int = 4):
     return out
 
 
-def annulus_tracers(n: int, seed: int = 5, r_in: float = 1.0, r_out: float = 6.0):
-    """n tracer positions uniform in area over the annulus r_in < r < r_out."""
+def annulus_tracers(n: int, seed: int = 5, r_in: float = 1.0, r_out: float = 6.0, mesh=None):
+    """n tracer positions uniform in area over the annulus r_in < r < r_out.
+    With `mesh`, they are ordered by the mesh row and column they fall in, so
+    that neighbouring tracers read neighbouring cells (the advection kernel's
+    gathers then share cache lines)."""
     import numpy as np
     rng = np.random.default_rng(seed)
     r = np.sqrt(rng.uniform(r_in * r_in, r_out * r_out, n))
     phi = rng.uniform(0.0, 2.0 * np.pi, n)
-    return np.stack([r * np.cos(phi), r * np.sin(phi)], axis=1)
+    xy = np.stack([r * np.cos(phi), r * np.sin(phi)], axis=1)
+    if mesh is not None:
+        R, dx, N = mesh.domain_radius, mesh.cell_spacing(), mesh.zones_per_side()
+        i = np.clip(((xy[:, 0] + R) / dx).astype(np.int64), 0, N - 1)
+        j = np.clip(((xy[:, 1] + R) / dx).astype(np.int64), 0, N - 1)
+        xy = xy[np.argsort(i * N + j, kind="stable")]
+    return xy
 
 
 def disk_8192(seed: int = 5):

@@ -761,23 +761,29 @@ static b2d_status launch_stage(b2d_ctx* ctx, const StagePlan& sp, int stage, int
 // input, bilinear between the four surrounding cell centres of the uniform
 // mesh, advanced by the same RK stages and weighted averages as the state and
 // wrapped into the periodic domain [-R, R)^2.  Positions are FP64.
-template <int NF, int STORE>
-__device__ __forceinline__ void tracer_cell_velocity(const RunDev& rd, int slot, int i, int j, double& vx, double& vy)
+// Gas velocity of one cell.  R = double is the FP64 parity arithmetic; the
+// FP32 paths interpolate in FP32 (the FP64 divisions would dominate on this
+// GPU) and keep the positions in FP64.
+template <class R, int STORE>
+__device__ __forceinline__ void tracer_cell_velocity(const RunDev& rd, int slot, int i, int j, R& vx, R& vy)
 {
     const size_t nn = (size_t)rd.N * rd.N, idx = (size_t)i * rd.N + j;
-    double u[3];
+    R u[3];
     for (int f = 0; f < 3; ++f) {
-        if (STORE == 0) u[f] = ((const double*)rd.slot[slot])[f * nn + idx];
-        else {
-            const float* p = (const float*)rd.slot[slot];
-            u[f] = (double)p[(2 * f) * nn + idx] + (double)p[(2 * f + 1) * nn + idx];
-        }
+        if (STORE == 0) u[f] = (R)((const double*)rd.slot[slot])[f * nn + idx];
+        else u[f] = (R)((const float*)rd.slot[slot])[(2 * f) * nn + idx];
     }
-    vx = u[1] / u[0];
-    vy = u[2] / u[0];
+    if constexpr (std::is_same<R, double>::value) {
+        vx = u[1] / u[0];
+        vy = u[2] / u[0];
+    } else {
+        const float ir = __fdividef(1.0f, u[0]);
+        vx = u[1] * ir;
+        vy = u[2] * ir;
+    }
 }
 
-template <int NF, int STORE>
+template <class R, int STORE>
 __global__ void tracer_kernel(const RunDev* runs, int run, int in_slot, int base_slot, int out_slot, double bf)
 {
     const RunDev& rd = runs[run];
@@ -788,20 +794,21 @@ __global__ void tracer_kernel(const RunDev* runs, int run, int in_slot, int base
     const double x = rd.tracers[in_slot][2 * k], y = rd.tracers[in_slot][2 * k + 1];
     const double gx = (x + R) / dx - 0.5, gy = (y + R) / dx - 0.5;
     const double fi = floor(gx), fj = floor(gy);
-    const double ax = gx - fi, ay = gy - fj;
+    const R ax = (R)(gx - fi), ay = (R)(gy - fj);
     int i0 = (int)fi, j0 = (int)fj;
     i0 = ((i0 % N) + N) % N;
     j0 = ((j0 % N) + N) % N;
     const int i1 = i0 + 1 == N ? 0 : i0 + 1, j1 = j0 + 1 == N ? 0 : j0 + 1;
-    double v00x, v00y, v10x, v10y, v01x, v01y, v11x, v11y;
-    tracer_cell_velocity<NF, STORE>(rd, in_slot, i0, j0, v00x, v00y);
-    tracer_cell_velocity<NF, STORE>(rd, in_slot, i1, j0, v10x, v10y);
-    tracer_cell_velocity<NF, STORE>(rd, in_slot, i0, j1, v01x, v01y);
-    tracer_cell_velocity<NF, STORE>(rd, in_slot, i1, j1, v11x, v11y);
-    const double w00 = (1.0 - ax) * (1.0 - ay), w10 = ax * (1.0 - ay), w01 = (1.0 - ax) * ay, w11 = ax * ay;
-    const double vx = w00 * v00x + w10 * v10x + w01 * v01x + w11 * v11x;
-    const double vy = w00 * v00y + w10 * v10y + w01 * v01y + w11 * v11y;
-    double xo = x + dt * vx, yo = y + dt * vy;
+    R v00x, v00y, v10x, v10y, v01x, v01y, v11x, v11y;
+    tracer_cell_velocity<R, STORE>(rd, in_slot, i0, j0, v00x, v00y);
+    tracer_cell_velocity<R, STORE>(rd, in_slot, i1, j0, v10x, v10y);
+    tracer_cell_velocity<R, STORE>(rd, in_slot, i0, j1, v01x, v01y);
+    tracer_cell_velocity<R, STORE>(rd, in_slot, i1, j1, v11x, v11y);
+    const R one = R(1);
+    const R w00 = (one - ax) * (one - ay), w10 = ax * (one - ay), w01 = (one - ax) * ay, w11 = ax * ay;
+    const R vx = w00 * v00x + w10 * v10x + w01 * v01x + w11 * v11x;
+    const R vy = w00 * v00y + w10 * v10y + w01 * v01y + w11 * v11y;
+    double xo = x + dt * (double)vx, yo = y + dt * (double)vy;
     const double L = 2.0 * R;
     if (base_slot >= 0) {
         // average with the base position on the same periodic image
@@ -828,9 +835,12 @@ static b2d_status launch_tracers(b2d_ctx* ctx, const StagePlan& sp, bool count)
         if (n <= 0) continue;
         const int threads = 256;
         const unsigned grid = (unsigned)((n + threads - 1) / threads);
-        const int store = ctx->precision == B2D_PREC_FP32_COMP ? 1 : 0;
-        if (store == 0) tracer_kernel<3, 0><<<grid, threads, 0, ctx->stream>>>(ctx->rdev, r, sp.in, sp.base, sp.out, sp.bf);
-        else tracer_kernel<3, 1><<<grid, threads, 0, ctx->stream>>>(ctx->rdev, r, sp.in, sp.base, sp.out, sp.bf);
+        if (ctx->precision == B2D_PREC_FP64)
+            tracer_kernel<double, 0><<<grid, threads, 0, ctx->stream>>>(ctx->rdev, r, sp.in, sp.base, sp.out, sp.bf);
+        else if (ctx->precision == B2D_PREC_FP32_STATE64)
+            tracer_kernel<float, 0><<<grid, threads, 0, ctx->stream>>>(ctx->rdev, r, sp.in, sp.base, sp.out, sp.bf);
+        else
+            tracer_kernel<float, 1><<<grid, threads, 0, ctx->stream>>>(ctx->rdev, r, sp.in, sp.base, sp.out, sp.bf);
         CUDA_TRY(cudaGetLastError());
         if (count) ctx->launches++;
     }

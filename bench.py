@@ -216,7 +216,7 @@ def ours(args):
     zones = mesh.total_zones()
     cons = b2.initial_state(mesh, hydro, physics, model)
     run = b2.Run(mesh, hydro, physics)
-    tracers = b2.presets.annulus_tracers(args.tracers, seed=5 + rank) if args.tracers > 0 else None
+    tracers = b2.presets.annulus_tracers(args.tracers, seed=5 + rank, mesh=mesh) if args.tracers > 0 else None
 
     tuned = {}
 
@@ -332,8 +332,8 @@ def ours(args):
         nthreads = 2 * (os.cpu_count() or 1)
         v, n = cpu_sample(mesh, hydro, physics, model, args.cpu_seconds, nthreads)
         cpu = {"value": v, "unit": UNIT, "cores": nthreads, "kind": "port",
-               "sample": "%d RK2 steps of the same 2048^2 disk with the C oracle, %d threads on %d host cores"
-                         % (n, nthreads, os.cpu_count() or 1)}
+               "sample": "%d RK2 steps of the same %d^2 mesh with the C oracle, %d threads on %d host cores"
+                         % (n, mesh.zones_per_side(), nthreads, os.cpu_count() or 1)}
 
     if rank == 0:
         line = {
