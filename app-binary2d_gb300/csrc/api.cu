@@ -783,7 +783,7 @@ __device__ __forceinline__ void tracer_cell_velocity(const RunDev& rd, int slot,
     }
 }
 
-template <class R, int STORE>
+template <class T, int STORE>
 __global__ void tracer_kernel(const RunDev* runs, int run, int in_slot, int base_slot, int out_slot, double bf)
 {
     const RunDev& rd = runs[run];
@@ -794,20 +794,20 @@ __global__ void tracer_kernel(const RunDev* runs, int run, int in_slot, int base
     const double x = rd.tracers[in_slot][2 * k], y = rd.tracers[in_slot][2 * k + 1];
     const double gx = (x + R) / dx - 0.5, gy = (y + R) / dx - 0.5;
     const double fi = floor(gx), fj = floor(gy);
-    const R ax = (R)(gx - fi), ay = (R)(gy - fj);
+    const T ax = (T)(gx - fi), ay = (T)(gy - fj);
     int i0 = (int)fi, j0 = (int)fj;
     i0 = ((i0 % N) + N) % N;
     j0 = ((j0 % N) + N) % N;
     const int i1 = i0 + 1 == N ? 0 : i0 + 1, j1 = j0 + 1 == N ? 0 : j0 + 1;
-    R v00x, v00y, v10x, v10y, v01x, v01y, v11x, v11y;
-    tracer_cell_velocity<R, STORE>(rd, in_slot, i0, j0, v00x, v00y);
-    tracer_cell_velocity<R, STORE>(rd, in_slot, i1, j0, v10x, v10y);
-    tracer_cell_velocity<R, STORE>(rd, in_slot, i0, j1, v01x, v01y);
-    tracer_cell_velocity<R, STORE>(rd, in_slot, i1, j1, v11x, v11y);
-    const R one = R(1);
-    const R w00 = (one - ax) * (one - ay), w10 = ax * (one - ay), w01 = (one - ax) * ay, w11 = ax * ay;
-    const R vx = w00 * v00x + w10 * v10x + w01 * v01x + w11 * v11x;
-    const R vy = w00 * v00y + w10 * v10y + w01 * v01y + w11 * v11y;
+    T v00x, v00y, v10x, v10y, v01x, v01y, v11x, v11y;
+    tracer_cell_velocity<T, STORE>(rd, in_slot, i0, j0, v00x, v00y);
+    tracer_cell_velocity<T, STORE>(rd, in_slot, i1, j0, v10x, v10y);
+    tracer_cell_velocity<T, STORE>(rd, in_slot, i0, j1, v01x, v01y);
+    tracer_cell_velocity<T, STORE>(rd, in_slot, i1, j1, v11x, v11y);
+    const T one = T(1);
+    const T w00 = (one - ax) * (one - ay), w10 = ax * (one - ay), w01 = (one - ax) * ay, w11 = ax * ay;
+    const T vx = w00 * v00x + w10 * v10x + w01 * v01x + w11 * v11x;
+    const T vy = w00 * v00y + w10 * v10y + w01 * v01y + w11 * v11y;
     double xo = x + dt * (double)vx, yo = y + dt * (double)vy;
     const double L = 2.0 * R;
     if (base_slot >= 0) {
