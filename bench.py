@@ -352,8 +352,9 @@ def ours(args):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                          "frac": achieved / hbm_peak, "peak_kind": peak_kind,
                          "traffic": ncu_traffic(args.workload, prec),
-                         "traffic_note": "DRAM bytes of one first-stage launch (72 B/zone algorithmic, "
-                                         "302 MB) from profiles/stage2_kernel_fp32comp_disk2048.md",
+                         "traffic_note": ("DRAM bytes of one first-stage launch (72 B/zone algorithmic, "
+                                          "302 MB) from profiles/stage2_kernel_fp32comp_disk2048.md")
+                                         if ncu_traffic(args.workload, prec) else "no ncu capture of this workload",
                          "algorithmic_bytes_per_launch": bytes_per_launch,
                          "bytes_per_zone_update": bytes_per_zone_update, "stage_ms": stage_ms,
                          "limiter": "FP32 instruction issue (ncu: 71% issue active, DRAM 14% of peak)"},
