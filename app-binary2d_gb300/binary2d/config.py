@@ -96,16 +96,27 @@ class Physics:
         return self.sink_radius if self.softening_length is None else self.softening_length
 
 
+MODEL_KINDS = {"infinite_disk": 0, "infinite_alpha_disk": 1, "finite_disk": 2, "residual_test": 3}
+
+
 @dataclass
 class DiskModel:
-    """InfiniteDisk (disks.rs:137-157) plus the synthetic cavity and seeded
-    multiplicative Σ noise (neither is in the reference)."""
+    """An initial model of AnyModel (src/app.rs:41-48): `kind` is one of
+    infinite_disk (disks.rs:137-157), infinite_alpha_disk (172-193),
+    finite_disk (11-115; disk_mass, disk_width, disk_radius,
+    softening_length) or residual_test (208-228).  The synthetic cavity and
+    seeded multiplicative Σ noise are additions (the reference has neither)."""
     surface_density: float = 1.0
     mach_number: Optional[float] = None
     cavity_radius: float = 0.0
     cavity_floor: float = 1e-4
     noise: float = 0.0
     seed: int = 0
+    kind: str = "infinite_disk"
+    disk_mass: float = 0.0
+    disk_width: float = 1.0
+    disk_radius: float = 1.0
+    softening_length: float = 0.0
 
 
 def to_c(mesh: Mesh, hydro, physics: Physics) -> B2DConfig:

@@ -73,6 +73,12 @@ def initial_state(mesh: Mesh, hydro, physics: Physics, model: DiskModel, run: in
     m.noise = model.noise
     m.seed = model.seed
     m.run = run
+    from .config import MODEL_KINDS
+    m.kind = MODEL_KINDS[model.kind]
+    m.disk_mass = model.disk_mass
+    m.disk_width = model.disk_width
+    m.disk_radius = model.disk_radius
+    m.disk_softening = model.softening_length
     nf = num_fields(hydro)
     out = np.empty((mesh.num_blocks, mesh.num_blocks, mesh.block_size, mesh.block_size, nf), dtype=np.float64)
     _check(lib.b2d_initial_state(ctypes.byref(c), ctypes.byref(m), _dp(out)))

@@ -48,11 +48,67 @@ static double zone_uniform(uint64_t seed, int run, int gi, int gj)
     return (double)(h >> 11) * (1.0 / 9007199254740992.0);
 }
 
+// InitialModel::primitive_at of the reference's models (src/disks.rs):
+// (Σ, vx, vy, p) at (x, y) before the synthetic cavity and noise.
+static void model_primitive(const b2d_config* c, const b2d_disk_model* m, double x, double y, double* p)
+{
+    const double gm = c->hydro_kind == B2D_EULER ? c->gamma_law_index : 1.0;
+    const double r = std::sqrt(x * x + y * y);
+    // hydro.global_mach_number().or(model.mach_number): isothermal uses its own
+    const double mach = c->hydro_kind == B2D_ISOTHERMAL ? c->mach_number : m->mach_number;
+    double sd, vx, vy, pg;
+    if (m->kind == B2D_MODEL_INFINITE_ALPHA_DISK) {                  // disks.rs:172-193
+        sd = m->surface_density * std::pow(r, -3.0 / 5.0);
+        double vp = std::pow(r, -0.5);
+        vx = vp * (-y / r);
+        vy = vp * (x / r);
+        double ma = mach * std::pow(r, -1.0 / 20.0);
+        double cs = vp / ma;
+        pg = cs * cs * sd / gm;
+    } else if (m->kind == B2D_MODEL_FINITE_DISK) {                   // disks.rs:20-115
+        const double r0 = m->disk_radius, dr = m->disk_width, md = m->disk_mass, rs = m->disk_softening;
+        const double pi = 3.14159265358979323846;
+        const double q0 = r0 / dr;
+        const double total = pi * dr * dr * (std::exp(-(q0 * q0)) + std::sqrt(pi) * r0 / dr * (1.0 + std::erf(r0 / dr)));
+        const double sigma0 = md / total;
+        double vp = std::pow(r, -0.5);
+        vx = vp * (-y / r);
+        vy = vp * (x / r);
+        double z = (r - r0) / dr;
+        sd = sigma0 * std::exp(-(z * z));
+        double kep2 = 1.0 * 1.0 * r * r / std::pow(r * r + rs * rs, 1.5);
+        double cs2 = kep2 / (mach * mach);
+        pg = sd * cs2 / gm;
+    } else if (m->kind == B2D_MODEL_RESIDUAL_TEST) {                 // disks.rs:208-228
+        double phi = std::atan2(x, y);
+        double r1 = std::sqrt((x - 1.0) * (x - 1.0) + (y - 1.0) * (y - 1.0));
+        double r2 = std::sqrt((x + 1.0) * (x + 1.0) + (y + 1.0) * (y + 1.0));
+        sd = 1.0 + std::exp(-(r1 * r1));
+        pg = 1.0 + std::exp(-(r2 * r2));
+        double damp = std::exp(-5.0 / r - r * r / 3.0);
+        double vp = std::pow(r, -0.5) * damp;
+        double vr = std::sin(phi - 3.14159 / 4.0) * damp;
+        vx = vp * (-y / r) + vr * (x / r);
+        vy = vp * (x / r) + vr * (y / r);
+    } else {                                                          // disks.rs:137-157
+        sd = m->surface_density;
+        double vp = std::pow(r, -0.5);
+        vx = vp * (-y / r);
+        vy = vp * (x / r);
+        double cs = vp / mach;
+        pg = cs * cs * sd / gm;
+    }
+    p[0] = sd;
+    p[1] = vx;
+    p[2] = vy;
+    p[3] = pg;
+}
+
 }  // namespace b2d
 
-// BlockState::from_model (src/state.rs:74-86) with InfiniteDiskModel::primitive_at
-// (src/disks.rs:137-157): Σ constant, Keplerian v_φ = r^-1/2, c_s = v_φ / Mach,
-// p = c_s² Σ / γ; then the synthetic cavity and noise described in b2d.h.
+// BlockState::from_model (src/state.rs:74-86): the model's primitive at each
+// cell centre, then the synthetic cavity and noise described in b2d.h, then
+// to_conserved.
 extern "C" b2d_status b2d_initial_state(const b2d_config* c, const b2d_disk_model* m, double* cons)
 {
     if (!c || !m || !cons) return B2D_ERR_INVALID;
@@ -70,18 +126,20 @@ extern "C" b2d_status b2d_initial_state(const b2d_config* c, const b2d_disk_mode
                     for (int j = 0; j < bs; ++j) {
                         double x = xc[(size_t)bi * bs + i], y = xc[(size_t)bj * bs + j];
                         double r = std::sqrt(x * x + y * y);
-                        double sd = m->surface_density;
-                        if (m->cavity_radius > 0.0)
-                            sd = sd * std::fmax(m->cavity_floor, std::exp(-std::pow(m->cavity_radius / r, 12.0)));
+                        double p[4];
+                        b2d::model_primitive(c, m, x, y, p);
+                        double sd = p[0], vx = p[1], vy = p[2], pg = p[3];
+                        if (m->cavity_radius > 0.0) {
+                            double f = std::fmax(m->cavity_floor, std::exp(-std::pow(m->cavity_radius / r, 12.0)));
+                            sd = sd * f;
+                            pg = pg * f;
+                        }
                         if (m->noise != 0.0) {
                             double u = b2d::zone_uniform(m->seed, m->run, bi * bs + i, bj * bs + j);
-                            sd = sd * (1.0 + m->noise * (2.0 * u - 1.0));
+                            double f = 1.0 + m->noise * (2.0 * u - 1.0);
+                            sd = sd * f;
+                            pg = pg * f;
                         }
-                        double vp = std::pow(r, -0.5);
-                        double vx = vp * (-y / r);
-                        double vy = vp * (x / r);
-                        double cs = vp / mach;
-                        double pg = cs * cs * sd / gm;
                         double* u = cons + ((((size_t)bi * nb + bj) * bs + i) * bs + j) * nf;
                         u[0] = sd;
                         u[1] = sd * vx;

@@ -216,13 +216,27 @@ b2d_status b2d_max_signal_speed(b2d_ctx* ctx, int32_t run, double* out);
 
 /* ------------------------------------------------------------------------ */
 /* Initial conditions.  BlockState::from_model (src/state.rs:74-86) for the
- * InfiniteDisk model (src/disks.rs:137-157), extended by a synthetic cavity
- * and seeded multiplicative noise (both new: the reference has neither):
- *   Σ = surface_density · max(cavity_floor, exp(-(cavity_radius / r)^12))
- *       · (1 + noise · (2u - 1)),  u ~ U[0,1) from a counter hash of
+ * reference's initial models (AnyModel, src/app.rs:41-48):
+ *   B2D_MODEL_INFINITE_DISK        disks.rs:137-157
+ *   B2D_MODEL_INFINITE_ALPHA_DISK  disks.rs:172-193
+ *   B2D_MODEL_FINITE_DISK          disks.rs:11-115 (disk_mass, disk_width,
+ *                                  disk_radius, disk_softening)
+ *   B2D_MODEL_RESIDUAL_TEST        disks.rs:208-228
+ * optionally modified by a synthetic cavity and seeded multiplicative noise
+ * (both new: the reference has neither):
+ *   Σ ← Σ · max(cavity_floor, exp(-(cavity_radius / r)^12))
+ *         · (1 + noise · (2u - 1)),  u ~ U[0,1) from a counter hash of
  *   (seed, run, global zone i, global zone j).
  * cavity_radius = 0 disables the cavity; noise = 0 disables the noise.  The
- * result is written in block layout.  Runs on the host. */
+ * model's Mach number is used where the hydro has none (Euler).  The result
+ * is written in block layout.  Runs on the host. */
+enum {
+    B2D_MODEL_INFINITE_DISK = 0,
+    B2D_MODEL_INFINITE_ALPHA_DISK = 1,
+    B2D_MODEL_FINITE_DISK = 2,
+    B2D_MODEL_RESIDUAL_TEST = 3
+};
+
 typedef struct b2d_disk_model {
     double   surface_density;
     double   mach_number;      /* model Mach number (Euler); isothermal uses the hydro's */
@@ -231,7 +245,11 @@ typedef struct b2d_disk_model {
     double   noise;
     uint64_t seed;
     int32_t  run;
-    int32_t  pad_;
+    int32_t  kind;             /* B2D_MODEL_*                                 */
+    double   disk_mass;        /* finite disk                                 */
+    double   disk_width;
+    double   disk_radius;
+    double   disk_softening;
 } b2d_disk_model;
 
 b2d_status b2d_initial_state(const b2d_config* cfg, const b2d_disk_model* model,

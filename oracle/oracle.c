@@ -1078,32 +1078,85 @@ static double zone_uniform(uint64_t seed, int run, int gi, int gj)
     return (double)(h >> 11) * (1.0 / 9007199254740992.0);
 }
 
+/* InitialModel::primitive_at (disks.rs): InfiniteDisk 137-157,
+ * InfiniteAlphaDisk 172-193, FiniteDisk 20-115, ResidualTest 208-228. */
+static void model_primitive(const oracle_config* c, const oracle_disk_model* m, double x, double y, double* p)
+{
+    double gm = c->hydro_kind == 1 ? c->gamma_law_index : 1.0;
+    double r = sqrt(x * x + y * y);
+    double mach = c->hydro_kind == 0 ? c->mach_number : m->mach_number;
+    double sd, vx, vy, pg;
+    if (m->kind == 1) {
+        sd = m->surface_density * pow(r, -3.0 / 5.0);
+        double vp = pow(r, -0.5);
+        vx = vp * (-y / r);
+        vy = vp * (x / r);
+        double ma = mach * pow(r, -1.0 / 20.0);
+        double cs = vp / ma;
+        pg = cs * cs * sd / gm;
+    } else if (m->kind == 2) {
+        double r0 = m->disk_radius, dr = m->disk_width, md = m->disk_mass, rs = m->disk_softening;
+        double pi = 3.14159265358979323846;
+        double q0 = r0 / dr;
+        double total = pi * dr * dr * (exp(-(q0 * q0)) + sqrt(pi) * r0 / dr * (1.0 + erf(r0 / dr)));
+        double sigma0 = md / total;
+        double vp = pow(r, -0.5);
+        vx = vp * (-y / r);
+        vy = vp * (x / r);
+        double z = (r - r0) / dr;
+        sd = sigma0 * exp(-(z * z));
+        double kep2 = 1.0 * 1.0 * r * r / pow(r * r + rs * rs, 1.5);
+        double cs2 = kep2 / (mach * mach);
+        pg = sd * cs2 / gm;
+    } else if (m->kind == 3) {
+        double phi = atan2(x, y);
+        double r1 = sqrt((x - 1.0) * (x - 1.0) + (y - 1.0) * (y - 1.0));
+        double r2 = sqrt((x + 1.0) * (x + 1.0) + (y + 1.0) * (y + 1.0));
+        sd = 1.0 + exp(-(r1 * r1));
+        pg = 1.0 + exp(-(r2 * r2));
+        double damp = exp(-5.0 / r - r * r / 3.0);
+        double vp = pow(r, -0.5) * damp;
+        double vr = sin(phi - 3.14159 / 4.0) * damp;
+        vx = vp * (-y / r) + vr * (x / r);
+        vy = vp * (x / r) + vr * (y / r);
+    } else {
+        sd = m->surface_density;
+        double vp = pow(r, -0.5);
+        vx = vp * (-y / r);
+        vy = vp * (x / r);
+        double cs = vp / mach;
+        pg = cs * cs * sd / gm;
+    }
+    p[0] = sd;
+    p[1] = vx;
+    p[2] = vy;
+    p[3] = pg;
+}
+
 int oracle_initial_state(const oracle_config* c, const oracle_disk_model* m, double* cons)
 {
     int nf = nfields(c), nb = c->num_blocks, bs = c->block_size;
     double* xc = malloc(sizeof(double) * nb * bs);
     for (int b = 0; b < nb; ++b) oracle_cell_centers(c, b, xc + b * bs);
-    double gm = c->hydro_kind == 1 ? c->gamma_law_index : 1.0;
-    double mach = c->hydro_kind == 0 ? c->mach_number : m->mach_number;
     for (int bi = 0; bi < nb; ++bi)
         for (int bj = 0; bj < nb; ++bj)
             for (int i = 0; i < bs; ++i)
                 for (int j = 0; j < bs; ++j) {
                     double x = xc[bi * bs + i], y = xc[bj * bs + j];
                     double r = sqrt(x * x + y * y);
-                    double sd = m->surface_density;
-                    if (m->cavity_radius > 0.0)
-                        sd = sd * fmax(m->cavity_floor, exp(-pow(m->cavity_radius / r, 12.0)));
+                    double p[4];
+                    model_primitive(c, m, x, y, p);
+                    if (m->cavity_radius > 0.0) {
+                        double f = fmax(m->cavity_floor, exp(-pow(m->cavity_radius / r, 12.0)));
+                        p[0] = p[0] * f;
+                        p[3] = p[3] * f;
+                    }
                     if (m->noise != 0.0) {
                         double u = zone_uniform(m->seed, m->run, bi * bs + i, bj * bs + j);
-                        sd = sd * (1.0 + m->noise * (2.0 * u - 1.0));
+                        double f = 1.0 + m->noise * (2.0 * u - 1.0);
+                        p[0] = p[0] * f;
+                        p[3] = p[3] * f;
                     }
-                    double vp = pow(r, -0.5);
-                    double vx = vp * (-y / r);
-                    double vy = vp * (x / r);
-                    double cs = vp / mach;
-                    double pg = cs * cs * sd / gm;
-                    double p[4] = {sd, vx, vy, pg};
                     size_t z = (((size_t)(bi * nb + bj) * bs + i) * bs + j) * nf;
                     prim_to_cons(c, p, cons + z);
                 }

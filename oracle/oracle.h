@@ -86,7 +86,11 @@ typedef struct oracle_disk_model {
     double   noise;
     uint64_t seed;
     int32_t  run;
-    int32_t  pad_;
+    int32_t  kind;   /* 0 infinite, 1 infinite alpha, 2 finite, 3 residual test */
+    double   disk_mass;
+    double   disk_width;
+    double   disk_radius;
+    double   disk_softening;
 } oracle_disk_model;
 
 /* m, x, y, vx, vy of each body */
