@@ -84,6 +84,8 @@ _SIGNATURES = [
     ("b2d_pin_host", c_int32, [ctypes.c_void_p, ctypes.c_uint64]),
     ("b2d_unpin_host", c_int32, [ctypes.c_void_p]),
     ("b2d_set_device", c_int32, [c_int32]),
+    ("b2d_download_elements", c_int32, [ctypes.c_void_p, c_int32, c_dp]),
+    ("b2d_upload_elements", c_int32, [ctypes.c_void_p, c_int32, c_dp]),
     ("b2d_set_tracers", c_int32, [ctypes.c_void_p, c_int32, c_int64, c_dp]),
     ("b2d_get_tracers", c_int32, [ctypes.c_void_p, c_int32, c_dp]),
     ("b2d_stage_noalloc", c_int32, [ctypes.POINTER(B2DConfig), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,

@@ -409,12 +409,15 @@ class Driver:
     def _load(self, rt):
         s = self.app.state
         rt.upload(0, s.cons, background=self.background, ledger=s.ledger, time=s.time, iteration=s.iteration)
+        if s.elements is not None:
+            rt.upload_elements(0, s.elements)
         self._active = rt
 
     def _store(self, rt):
         s = self.app.state
         s.cons, s.time, s.iteration = rt.download(0)
         s.ledger = rt.ledger(0)
+        s.elements = rt.elements(0)
 
     # -- side effects (main.rs:27-86) ------------------------------------------------
     def side_effects(self, rt):

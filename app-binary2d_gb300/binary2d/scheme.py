@@ -154,6 +154,17 @@ class Runtime:
         _check(self.lib.b2d_download_ledger(self.ctx, run, _dp(out)))
         return out
 
+    def elements(self, run: int = 0) -> np.ndarray:
+        """Per-block orbital_elements_change [nb, nb, 7, 4] of (a, M, q, e)."""
+        m = self.runs[run].mesh
+        out = np.empty((m.num_blocks, m.num_blocks, 7, 4), dtype=np.float64)
+        _check(self.lib.b2d_download_elements(self.ctx, run, _dp(out)))
+        return out
+
+    def upload_elements(self, run: int, elements: np.ndarray):
+        e = np.ascontiguousarray(elements, dtype=np.float64)
+        _check(self.lib.b2d_upload_elements(self.ctx, run, _dp(e)))
+
     def set_tracers(self, run: int, xy: np.ndarray):
         """Massless tracers of a run: `xy` of shape [n, 2]."""
         xy = np.ascontiguousarray(xy, dtype=np.float64).reshape(-1, 2)

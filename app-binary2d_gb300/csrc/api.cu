@@ -211,6 +211,7 @@ struct RunHost {
     void* slot[NSLOTS] = {};
     void* bg = nullptr;
     double* ledger[NSLOTS] = {};
+    double* elements[NSLOTS] = {};
     double* partial = nullptr;
     unsigned* counter = nullptr;
     double *xc = nullptr, *xv = nullptr;
@@ -378,7 +379,7 @@ static void free_ctx(b2d_ctx* ctx)
     if (!ctx) return;
     for (auto& kv : ctx->graphs) cudaGraphExecDestroy(kv.second);
     for (RunHost& r : ctx->runs) {
-        for (int s = 0; s < NSLOTS; ++s) { cudaFree(r.slot[s]); cudaFree(r.ledger[s]); }
+        for (int s = 0; s < NSLOTS; ++s) { cudaFree(r.slot[s]); cudaFree(r.ledger[s]); cudaFree(r.elements[s]); }
         const size_t ri = &r - ctx->runs.data();
         if (ri < ctx->rdev_h.size())
             for (int s = 0; s < NSLOTS; ++s) cudaFree(ctx->rdev_h[ri].tracers[s]);
@@ -513,6 +514,8 @@ extern "C" b2d_ctx* b2d_create(const b2d_config* cfgs, int32_t nruns, int32_t pr
             CREATE_TRY(cudaMemset(r.slot[s], 0, r.state_bytes));
             CREATE_TRY(cudaMalloc(&r.ledger[s], sizeof(double) * r.nblocks * NITEMS * ctx->nf));
             CREATE_TRY(cudaMemset(r.ledger[s], 0, sizeof(double) * r.nblocks * NITEMS * ctx->nf));
+            CREATE_TRY(cudaMalloc(&r.elements[s], sizeof(double) * r.nblocks * NITEMS * 4));
+            CREATE_TRY(cudaMemset(r.elements[s], 0, sizeof(double) * r.nblocks * NITEMS * 4));
         }
         CREATE_TRY(cudaMalloc(&r.bg, r.state_bytes));
         CREATE_TRY(cudaMemset(r.bg, 0, r.state_bytes));
@@ -537,7 +540,19 @@ extern "C" b2d_ctx* b2d_create(const b2d_config* cfgs, int32_t nruns, int32_t pr
 
         d.N = r.N; d.bs = r.bs; d.nb = r.nb; d.nblocks = r.nblocks;
         d.xc = r.xc; d.xv = r.xv; d.xcf = r.xcf; d.xvf = r.xvf;
-        for (int s = 0; s < NSLOTS; ++s) { d.slot[s] = r.slot[s]; d.ledger[s] = r.ledger[s]; }
+        for (int s = 0; s < NSLOTS; ++s) {
+            d.slot[s] = r.slot[s];
+            d.ledger[s] = r.ledger[s];
+            d.elements[s] = r.elements[s];
+        }
+        // OrbitalElements of the run (physics.rs:411-417)
+        if (cfgs[i].one_body) { d.el0[0] = 1e-12; d.el0[1] = 1.0; d.el0[2] = 1.0; d.el0[3] = 0.0; }
+        else {
+            d.el0[0] = 1.0;
+            d.el0[1] = 1.0;
+            d.el0[2] = cfgs[i].binary_mass_ratio;
+            d.el0[3] = cfgs[i].binary_eccentricity;
+        }
         d.bg = r.bg;
         d.time = ctx->d_time + (size_t)i * NSLOTS;
         d.iter = ctx->d_iter + (size_t)i * NSLOTS;
@@ -614,6 +629,7 @@ extern "C" b2d_status b2d_upload_state(b2d_ctx* ctx, int32_t run, const double* 
     size_t nled = (size_t)r.nblocks * NITEMS * ctx->nf;
     if (ledger) CUDA_TRY(cudaMemcpyAsync(r.ledger[ctx->cur], ledger, nled * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
     else CUDA_TRY(cudaMemsetAsync(r.ledger[ctx->cur], 0, nled * sizeof(double), ctx->stream));
+    CUDA_TRY(cudaMemsetAsync(r.elements[ctx->cur], 0, sizeof(double) * r.nblocks * NITEMS * 4, ctx->stream));
     long long it = iteration_num;
     CUDA_TRY(cudaMemcpyAsync(ctx->d_time + (size_t)run * NSLOTS + ctx->cur, &time, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
     CUDA_TRY(cudaMemcpyAsync(ctx->d_iter + (size_t)run * NSLOTS + ctx->cur, &it, sizeof(long long), cudaMemcpyHostToDevice, ctx->stream));
@@ -980,6 +996,17 @@ static b2d_status decode_failure(b2d_ctx* ctx, unsigned long long key, const std
     e->run = run;
     RunHost& r = ctx->runs[run];
     const int nb = r.nb, bs = r.bs;
+    double orb[10];
+    if (e->code == B2D_ERR_UNBOUND_ORBIT) {
+        // OrbitalEvolutionError is reported at position (0, 0) (scheme.rs:308-309);
+        // the failing block's index is carried in the zone field.
+        e->block_i = zone / nb;
+        e->block_j = zone % nb;
+        CUDA_TRY(cudaMemcpy(&e->time, r.stage_time + stage, sizeof(double), cudaMemcpyDeviceToHost));
+        CUDA_TRY(cudaMemcpy(orb, r.orbit + 10 * stage, sizeof orb, cudaMemcpyDeviceToHost));
+        e->binary[0] = orb[1]; e->binary[1] = orb[2]; e->binary[2] = orb[6]; e->binary[3] = orb[7];
+        return B2D_OK;
+    }
     const int bi = blk / nb, bj = blk % nb, di = order / 3 - 1, dj = order % 3 - 1;
     e->block_i = (bi + di + nb) % nb;
     e->block_j = (bj + dj + nb) % nb;
@@ -1002,7 +1029,6 @@ static b2d_status decode_failure(b2d_ctx* ctx, unsigned long long key, const std
         }
     }
     e->value = failure_value(r.cfg, u, e->code);
-    double orb[10];
     CUDA_TRY(cudaMemcpy(&e->time, r.stage_time + stage, sizeof(double), cudaMemcpyDeviceToHost));
     CUDA_TRY(cudaMemcpy(orb, r.orbit + 10 * stage, sizeof orb, cudaMemcpyDeviceToHost));
     e->binary[0] = orb[1]; e->binary[1] = orb[2]; e->binary[2] = orb[6]; e->binary[3] = orb[7];
@@ -1427,4 +1453,27 @@ extern "C" b2d_status b2d_stage_noalloc(const b2d_config* cfg, const double* d_i
     err.binary[0] = orb[1]; err.binary[1] = orb[2]; err.binary[2] = orb[6]; err.binary[3] = orb[7];
     if (err_out) *err_out = err;
     return fail((b2d_status)err.code, "hydro error in b2d_stage_noalloc");
+}
+
+// ---------------------------------------------------------------------------
+// Orbital-element change per block (BlockState::orbital_elements_change,
+// src/state.rs:44-49): [nb][nb][7][4] of (a, M, q, e) per ItemizedChange item.
+extern "C" b2d_status b2d_download_elements(b2d_ctx* ctx, int32_t run, double* elements)
+{
+    if (!ctx || run < 0 || run >= ctx->nruns || !elements) return fail(B2D_ERR_INVALID, "bad arguments");
+    RunHost& r = ctx->runs[run];
+    CUDA_TRY(cudaMemcpyAsync(elements, r.elements[ctx->cur], sizeof(double) * r.nblocks * NITEMS * 4,
+                             cudaMemcpyDeviceToHost, ctx->stream));
+    CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return B2D_OK;
+}
+
+extern "C" b2d_status b2d_upload_elements(b2d_ctx* ctx, int32_t run, const double* elements)
+{
+    if (!ctx || run < 0 || run >= ctx->nruns || !elements) return fail(B2D_ERR_INVALID, "bad arguments");
+    RunHost& r = ctx->runs[run];
+    CUDA_TRY(cudaMemcpyAsync(r.elements[ctx->cur], elements, sizeof(double) * r.nblocks * NITEMS * 4,
+                             cudaMemcpyHostToDevice, ctx->stream));
+    CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return B2D_OK;
 }

@@ -31,6 +31,8 @@ struct RunDev {
     double* orbit;           // [max_stages][10]: m, x, y, vx, vy of body 1 then body 2
     unsigned long long* amax;
     double binary_q, binary_e;
+    double* elements[NSLOTS];    // [nblocks][7][4] orbital-element change per slot (nullptr: not tracked)
+    double el0[4];               // unperturbed elements (a, M, q, e), physics.rs:411-417
     long long ntracers;          // massless tracer particles of this run (0: none)
     double* tracers[NSLOTS];     // [ntracers][2] positions (x, y) per state slot
     DevParams p;     // FP64 kernels

@@ -553,15 +553,21 @@ __global__ void __launch_bounds__(160, (NF == 3 && STORE == 1) ? 4 : 3) stage2_k
         const double* lin = rd.ledger[a.in_slot] + (size_t)block * NL;
         const double* lbase = has_base ? rd.ledger[a.base_slot] + (size_t)block * NL : nullptr;
         double* lout = rd.ledger[a.out_slot] + (size_t)block * NL;
+        __shared__ double s_ds[NITEMS * 4];
         for (int k = t; k < NL; k += NT) {
             double s = 0.0;
             for (int q = 0; q < rd.tiles_per_block; ++q)
                 s += __ldcg(rd.partial + ((size_t)block * rd.tiles_per_block + q) * NL + k);
+            s_ds[k] = s * area;
             double v = __ldcg(lin + k) + s * area;
             if (lbase) v = v * (-a.bf + 1.0) + __ldcg(lbase + k) * a.bf;
             lout[k] = v;
         }
-        if (t == 0) rd.counter[block] = 0u;
+        __syncthreads();
+        if (t == 0) {
+            finalize_elements<NF>(a, rd, ri, block, s_ds);
+            rd.counter[block] = 0u;
+        }
     }
 }
 

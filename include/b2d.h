@@ -186,6 +186,13 @@ b2d_status b2d_download_state(b2d_ctx* ctx, int32_t run, double* cons,
  * (BlockState::integrated_source_terms, src/state.rs:44-49). */
 b2d_status b2d_download_ledger(b2d_ctx* ctx, int32_t run, double* ledger);
 
+/* Per-block orbital-element change (BlockState::orbital_elements_change,
+ * src/state.rs:44-49; ItemizedChange::perturbation, state.rs:258-281):
+ * [num_blocks][num_blocks][7][4] of (a, M, q, e) per ledger item.  Uploading
+ * a state resets it to zero; these calls move it to and from the host. */
+b2d_status b2d_download_elements(b2d_ctx* ctx, int32_t run, double* elements);
+b2d_status b2d_upload_elements(b2d_ctx* ctx, int32_t run, const double* elements);
+
 /* ------------------------------------------------------------------------ */
 /* The step.  scheme::advance (src/scheme.rs:323-349): dt = cfl·dx / max
  * signal speed (floored by dt_min), then `fold` RK steps of

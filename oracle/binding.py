@@ -39,7 +39,7 @@ def load():
         vp = ctypes.c_void_p
         lib.oracle_advance.restype = c_int32
         lib.oracle_advance.argtypes = [vp, c_dp, c_dp, c_dp, c_dp, ctypes.POINTER(ctypes.c_int64), c_int32, c_dp,
-                                       c_int32, ctypes.POINTER(OracleError), c_dp, ctypes.c_int64]
+                                       c_int32, ctypes.POINTER(OracleError), c_dp, ctypes.c_int64, c_dp]
         lib.oracle_max_signal_speed.restype = c_double
         lib.oracle_max_signal_speed.argtypes = [vp, c_dp]
         lib.oracle_initial_state.restype = c_int32
@@ -78,15 +78,16 @@ class OracleHydroError(RuntimeError):
 
 class OracleState:
     """State (src/state.rs:57-62) held by the oracle: conserved in block layout,
-    per-block ledger, time, iteration."""
+    per-block ledger, per-block orbital-element change, time, iteration."""
 
-    def __init__(self, cfg, cons, background=None, ledger=None, time=0.0, iteration=0):
+    def __init__(self, cfg, cons, background=None, ledger=None, time=0.0, iteration=0, elements=None):
         self.cfg = cfg
         self.cons = np.array(cons, dtype=np.float64, copy=True)
         self.background = self.cons.copy() if background is None else np.ascontiguousarray(background, np.float64)
         nb = cfg.num_blocks
         nf = self.cons.shape[-1]
         self.ledger = np.zeros((nb, nb, 7, nf)) if ledger is None else np.array(ledger, dtype=np.float64)
+        self.elements = np.zeros((nb, nb, 7, 4)) if elements is None else np.array(elements, dtype=np.float64)
         self.time = ctypes.c_double(time)
         self.iteration = ctypes.c_int64(iteration)
         self.tracers = None
@@ -104,7 +105,7 @@ class OracleState:
         rc = lib.oracle_advance(ctypes.byref(self.cfg), _dp(self.cons), _dp(self.ledger), _dp(self.background),
                                 ctypes.byref(self.time), ctypes.byref(self.iteration), int(fold), ctypes.byref(dt),
                                 int(nthreads), ctypes.byref(err), None if tr is None else _dp(tr),
-                                0 if tr is None else len(tr))
+                                0 if tr is None else len(tr), _dp(self.elements))
         if rc:
             raise OracleHydroError(err)
         return dt.value

@@ -621,6 +621,9 @@ typedef struct stage_ctx {
     double* fys;            /* per block y fluxes bs*(bs+1)*nf */
     double* xc;             /* [nb][bs] cell centres */
     double* xv;             /* [nb][bs+1] vertices */
+    const double* el_in;    /* orbital_elements_change of the stage input, [nb][nb][7][4] */
+    double* el_out;         /* ... of the stage output (NULL: not tracked) */
+    int* unbound;           /* per block: its perturbed orbit is unbound */
 } stage_ctx;
 
 /* Phase A: try_block_primitive, scheme.rs:185-199 */
@@ -732,6 +735,61 @@ static void task_fluxes(pool* pl, int w, int b)
 #undef CD
 }
 
+/* OrbitalElements::perturb (kepler-two-body, un-vendored; restated from
+ * two-body mechanics).  At the orbital state `o`, body 1 gains mass dm1 and
+ * momentum (dpx1, dpy1) and body 2 gains dm2 and (dpx2, dpy2), each at a
+ * fixed position; the new elements follow from the relative orbit:
+ * M' = m1' + m2', q' = m2' / m1', E = |v|^2 / 2 - M' / |r|, a' = -M' / (2E),
+ * h = r x v, e' = sqrt(1 + 2 E h^2 / M'^2).  Returns 0 for E >= 0
+ * (UnboundOrbitalState, physics.rs:34-35), else writes (a', M', q', e') - el. */
+static int perturb(const orbit* o, const double* el, double dm1, double dm2, double dpx1, double dpx2,
+                   double dpy1, double dpy2, double* de)
+{
+    double m1 = o->p1.m + dm1, m2 = o->p2.m + dm2;
+    double u1x = (o->p1.m * o->p1.vx + dpx1) / m1, u1y = (o->p1.m * o->p1.vy + dpy1) / m1;
+    double u2x = (o->p2.m * o->p2.vx + dpx2) / m2, u2y = (o->p2.m * o->p2.vy + dpy2) / m2;
+    double M = m1 + m2;
+    double rx = o->p2.x - o->p1.x, ry = o->p2.y - o->p1.y;
+    double vx = u2x - u1x, vy = u2y - u1y;
+    double r = sqrt(rx * rx + ry * ry);
+    double E = 0.5 * (vx * vx + vy * vy) - M / r;
+    if (!(E < 0.0)) return 0;
+    double h = rx * vy - ry * vx;
+    double e2 = 1.0 + 2.0 * E * h * h / (M * M);
+    de[0] = -M / (2.0 * E) - el[0];
+    de[1] = M - el[1];
+    de[2] = m2 / m1 - el[2];
+    de[3] = (e2 > 0.0 ? sqrt(e2) : 0.0) - el[3];
+    return 1;
+}
+
+/* Physics::orbital_elements (physics.rs:411-417): (a, M, q, e). */
+static void unperturbed_elements(const oracle_config* c, double* el)
+{
+    if (c->one_body) { el[0] = 1e-12; el[1] = 1.0; el[2] = 1.0; el[3] = 0.0; }
+    else { el[0] = 1.0; el[1] = 1.0; el[2] = c->binary_mass_ratio; el[3] = c->binary_eccentricity; }
+}
+
+/* ItemizedChange::perturbation, state.rs:258-281: the sink and gravity items
+ * of the gas are taken from the bodies (negated), buffer, cooling and fake
+ * mass leave the orbit alone.  ds holds the block's sums times dx dy. */
+static int block_perturbation(const oracle_config* c, const orbit* o, const double* ds, int nf, double* de)
+{
+    double el[4];
+    unperturbed_elements(c, el);
+    for (int k = 0; k < NITEMS * 4; ++k) de[k] = 0.0;
+    const double* s1 = ds + SINK1 * nf;
+    const double* s2 = ds + SINK2 * nf;
+    const double* g1 = ds + GRAV1 * nf;
+    const double* g2 = ds + GRAV2 * nf;
+    int ok = 1;
+    ok &= perturb(o, el, -s1[0], 0.0, -s1[1], 0.0, -s1[2], 0.0, de + SINK1 * 4);
+    ok &= perturb(o, el, 0.0, -s2[0], 0.0, -s2[1], 0.0, -s2[2], de + SINK2 * 4);
+    ok &= perturb(o, el, -g1[0], 0.0, -g1[1], 0.0, -g1[2], 0.0, de + GRAV1 * 4);
+    ok &= perturb(o, el, 0.0, -g2[0], 0.0, -g2[1], 0.0, -g2[2], de + GRAV2 * 4);
+    return ok;
+}
+
 /* Phase C: compute_block_updated_solution, scheme.rs:273-317 */
 static void task_update(pool* pl, int w, int b)
 {
@@ -771,11 +829,18 @@ static void task_update(pool* pl, int w, int b)
             for (int k = 0; k < NITEMS * nf; ++k) ds[k] = ds[k] + it[k];
         }
     }
+    double area = dx * dy;
+    for (int k = 0; k < NITEMS * nf; ++k) ds[k] = ds[k] * area;
     if (s->led_out) {
-        double area = dx * dy;
         for (int k = 0; k < NITEMS * nf; ++k)
-            s->led_out[(size_t)b * NITEMS * nf + k] =
-                s->led_in[(size_t)b * NITEMS * nf + k] + ds[k] * area;
+            s->led_out[(size_t)b * NITEMS * nf + k] = s->led_in[(size_t)b * NITEMS * nf + k] + ds[k];
+    }
+    /* de = ds.perturbation(time, physics.orbital_elements()), scheme.rs:307-314 */
+    if (s->el_out) {
+        double de[NITEMS * 4];
+        s->unbound[b] = !block_perturbation(c, &s->o, ds, nf, de);
+        for (int k = 0; k < NITEMS * 4; ++k)
+            s->el_out[(size_t)b * NITEMS * 4 + k] = s->el_in[(size_t)b * NITEMS * 4 + k] + de[k];
     }
 }
 
@@ -788,6 +853,7 @@ typedef struct rk_state {
     double* cons;
     double* led;
     double* tr;       /* tracer positions [n][2] */
+    double* el;       /* orbital_elements_change [nb][nb][7][4] */
     double time;
     int64_t iteration;
 } rk_state;
@@ -847,11 +913,12 @@ static void advance_tracers(const stage_ctx* s, const double* cons_in, const dou
 }
 
 static void weighted_average(rk_state* s1, double bf, const rk_state* s0, size_t ncons,
-                             size_t nled)
+                             size_t nled, size_t nel)
 {
     double w1 = -bf + 1.0;
     for (size_t k = 0; k < ncons; ++k) s1->cons[k] = s1->cons[k] * w1 + s0->cons[k] * bf;
     for (size_t k = 0; k < nled; ++k) s1->led[k] = s1->led[k] * w1 + s0->led[k] * bf;
+    for (size_t k = 0; k < nel; ++k) s1->el[k] = s1->el[k] * w1 + s0->el[k] * bf;
     s1->time = s1->time * w1 + s0->time * bf;
 }
 
@@ -875,6 +942,8 @@ static int stage(advance_ctx* a, const rk_state* in, rk_state* out, const rk_sta
     s->led_in = in->led;
     s->cons_out = out->cons;
     s->led_out = out->led;
+    s->el_in = in->el;
+    s->el_out = out->el;
     a->pl->arg = s;
     int nblocks = s->nb * s->nb;
     pool_run(a->pl, nblocks, task_primitive);
@@ -911,6 +980,24 @@ static int stage(advance_ctx* a, const rk_state* in, rk_state* out, const rk_sta
     }
     pool_run(a->pl, nblocks, task_fluxes);
     pool_run(a->pl, nblocks, task_update);
+    /* An unbound orbit fails the stage after every block's primitives were
+     * converted: HydroErrorType::OrbitalEvolutionError at position (0, 0)
+     * with the binary's state (scheme.rs:308-309), first block in order. */
+    for (int b = 0; b < nblocks && s->el_out; ++b) {
+        if (s->unbound[b]) {
+            oracle_error* e = &a->err;
+            memset(e, 0, sizeof *e);
+            e->code = ORACLE_UNBOUND_ORBIT;
+            e->block_i = b / s->nb;
+            e->block_j = b % s->nb;
+            e->time = in->time;
+            e->binary[0] = s->o.p1.x;
+            e->binary[1] = s->o.p1.y;
+            e->binary[2] = s->o.p2.x;
+            e->binary[3] = s->o.p2.y;
+            return e->code;
+        }
+    }
     if (a->ntracers > 0)
         advance_tracers(s, in->cons, in->tr, base ? base->tr : NULL, bf, out->tr, a->ntracers);
     out->time = in->time + s->dt;
@@ -929,12 +1016,14 @@ double oracle_max_signal_speed(const oracle_config* c, const double* cons)
 
 int oracle_advance(const oracle_config* c, double* cons, double* ledger, const double* background,
                    double* time, int64_t* iteration, int32_t fold, double* dt_out,
-                   int32_t nthreads, oracle_error* err, double* tracers, int64_t ntracers)
+                   int32_t nthreads, oracle_error* err, double* tracers, int64_t ntracers,
+                   double* elements)
 {
     int nf = nfields(c), nb = c->num_blocks, bs = c->block_size;
     int nblocks = nb * nb;
     size_t ncons = (size_t)nblocks * bs * bs * nf;
     size_t nled = (size_t)nblocks * NITEMS * nf;
+    size_t nel = elements ? (size_t)nblocks * NITEMS * 4 : 0;
     if (nthreads < 1) nthreads = 1;
 
     /* dt, scheme.rs:336-340 */
@@ -963,6 +1052,7 @@ int oracle_advance(const oracle_config* c, double* cons, double* ledger, const d
     s->perr = calloc(nblocks, sizeof(int));
     s->pbad = calloc(nblocks, sizeof(double));
     s->pzone = calloc(nblocks, sizeof(int));
+    s->unbound = calloc(nblocks, sizeof(int));
     s->fxs = malloc(sizeof(double) * (size_t)nblocks * (bs + 1) * bs * nf);
     s->fys = malloc(sizeof(double) * (size_t)nblocks * (bs + 1) * bs * nf);
     size_t E = bs + 4;
@@ -977,7 +1067,9 @@ int oracle_advance(const oracle_config* c, double* cons, double* ledger, const d
         st[k].cons = malloc(sizeof(double) * ncons);
         st[k].led = calloc(nled, sizeof(double));
         st[k].tr = a.ntracers > 0 ? malloc(sizeof(double) * 2 * (size_t)a.ntracers) : NULL;
+        st[k].el = nel ? malloc(sizeof(double) * nel) : NULL;
     }
+    if (nel) memcpy(st[0].el, elements, sizeof(double) * nel);
     if (a.ntracers > 0) memcpy(st[0].tr, tracers, sizeof(double) * 2 * (size_t)a.ntracers);
     memcpy(st[0].cons, cons, sizeof(double) * ncons);
     if (ledger) memcpy(st[0].led, ledger, sizeof(double) * nled);
@@ -1011,7 +1103,7 @@ int oracle_advance(const oracle_config* c, double* cons, double* ledger, const d
             rc = stage(&a, s0, &st[1], NULL, 0.0);
             if (!rc) rc = stage(&a, &st[1], &st[2], s0, 0.5);
             if (!rc) {
-                weighted_average(&st[2], 0.5, s0, ncons, nled);      /* br = 1/2 */
+                weighted_average(&st[2], 0.5, s0, ncons, nled, nel);      /* br = 1/2 */
                 st[2].iteration = (st[2].iteration + s0->iteration) / 2;
                 rk_state t = st[0]; st[0] = st[2]; st[2] = t;
             }
@@ -1019,11 +1111,11 @@ int oracle_advance(const oracle_config* c, double* cons, double* ledger, const d
             rc = stage(&a, s0, &st[1], NULL, 0.0);
             if (!rc) rc = stage(&a, &st[1], &st[2], s0, 3.0 / 4.0);
             if (!rc) {
-                weighted_average(&st[2], 3.0 / 4.0, s0, ncons, nled); /* br = 3/4 */
+                weighted_average(&st[2], 3.0 / 4.0, s0, ncons, nled, nel); /* br = 3/4 */
                 rc = stage(&a, &st[2], &st[3], s0, 1.0 / 3.0);
             }
             if (!rc) {
-                weighted_average(&st[3], 1.0 / 3.0, s0, ncons, nled); /* br = 1/3 */
+                weighted_average(&st[3], 1.0 / 3.0, s0, ncons, nled, nel); /* br = 1/3 */
                 st[3].iteration = s0->iteration + 1;
                 rk_state t = st[0]; st[0] = st[3]; st[3] = t;
             }
@@ -1045,14 +1137,15 @@ int oracle_advance(const oracle_config* c, double* cons, double* ledger, const d
         *time = st[0].time;
         *iteration = st[0].iteration;
         if (a.ntracers > 0) memcpy(tracers, st[0].tr, sizeof(double) * 2 * (size_t)a.ntracers);
+        if (nel) memcpy(elements, st[0].el, sizeof(double) * nel);
     } else if (err) {
         *err = a.err;
     }
 
-    for (int k = 0; k < 4; ++k) { free(st[k].cons); free(st[k].led); free(st[k].tr); }
+    for (int k = 0; k < 4; ++k) { free(st[k].cons); free(st[k].led); free(st[k].tr); free(st[k].el); }
     for (int t = 0; t < nthreads; ++t) free(s->scratch[t]);
     free(s->scratch);
-    free(s->xc); free(s->xv); free(s->prim); free(s->perr); free(s->pbad); free(s->pzone);
+    free(s->xc); free(s->xv); free(s->prim); free(s->perr); free(s->pbad); free(s->pzone); free(s->unbound);
     free(s->fxs); free(s->fys);
     return rc;
 }

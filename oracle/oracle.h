@@ -99,14 +99,16 @@ typedef struct oracle_point_mass { double m, x, y, vx, vy; } oracle_point_mass;
 #define ORACLE_OK 0
 #define ORACLE_NEG_DENSITY 1
 #define ORACLE_NEG_PRESSURE 2
+#define ORACLE_UNBOUND_ORBIT 3
 
 /* scheme::advance: fold RK steps with one dt; cons [nb][nb][bs][bs][nf],
- * ledger [nb][nb][7][nf] (may be NULL), background like cons. */
+ * ledger [nb][nb][7][nf] (may be NULL), background like cons, elements the
+ * orbital_elements_change [nb][nb][7][4] of (a, M, q, e) (may be NULL). */
 int oracle_advance(const oracle_config* cfg, double* cons, double* ledger,
                    const double* background, double* time, int64_t* iteration,
                    int32_t fold, double* dt_out, int32_t nthreads,
                    oracle_error* err, double* tracers /* [n][2] or NULL */,
-                   int64_t ntracers);
+                   int64_t ntracers, double* elements /* or NULL */);
 
 double oracle_max_signal_speed(const oracle_config* cfg, const double* cons);
 

@@ -21,7 +21,7 @@ hydro:
 model:
   infinite_disk:
     mach_number: ~
-    surface_density: 1.0
+    surface_density: 1e-3  # light gas: a coarse block's pull keeps the binary bound
 mesh:
   block_size: 16
   num_blocks: 2
@@ -133,6 +133,12 @@ class FakeRuntime:
     def ledger(self, run=0):
         return self._led.copy()
 
+    def upload_elements(self, run, elements):
+        self._el = elements.copy()
+
+    def elements(self, run=0):
+        return getattr(self, "_el", np.zeros(self._led.shape[:2] + (7, 4))).copy()
+
     def time(self, run=0):
         return self.t, self.it
 
@@ -204,3 +210,5 @@ def test_checkpoint_restart_is_bitwise_continuous(tmp_path):
     assert rest.state.iteration == full.state.iteration
     assert np.array_equal(rest.state.cons, full.state.cons)
     assert np.array_equal(rest.state.ledger, full.state.ledger)
+    assert np.array_equal(rest.state.elements, full.state.elements)
+    assert np.abs(full.state.elements).max() > 0.0
