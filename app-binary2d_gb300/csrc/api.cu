@@ -14,6 +14,7 @@
 #include <string>
 #include <vector>
 
+#include "elements.cuh"
 #include "runtime.cuh"
 
 namespace b2d {
@@ -218,6 +219,8 @@ struct RunHost {
     float *xcf = nullptr, *xvf = nullptr;
     double* stage_time = nullptr;
     double* orbit = nullptr;
+    double* stage_ds = nullptr;
+    double* stage_de = nullptr;
     std::vector<double> hxc;
 };
 
@@ -385,7 +388,7 @@ static void free_ctx(b2d_ctx* ctx)
             for (int s = 0; s < NSLOTS; ++s) cudaFree(ctx->rdev_h[ri].tracers[s]);
         cudaFree(r.bg); cudaFree(r.partial); cudaFree(r.counter);
         cudaFree(r.xc); cudaFree(r.xv); cudaFree(r.xcf); cudaFree(r.xvf);
-        cudaFree(r.stage_time); cudaFree(r.orbit);
+        cudaFree(r.stage_time); cudaFree(r.orbit); cudaFree(r.stage_ds); cudaFree(r.stage_de);
     }
     cudaFree(ctx->rdev); cudaFree(ctx->d_dt); cudaFree(ctx->d_time); cudaFree(ctx->d_iter);
     cudaFree(ctx->d_amax); cudaFree(ctx->d_err_key); cudaFree(ctx->d_adv_count); cudaFree(ctx->d_timeout); cudaFree(ctx->d_staging);
@@ -429,12 +432,20 @@ static b2d_status ensure_stage_capacity(b2d_ctx* ctx, int fold)
         RunHost& r = ctx->runs[i];
         CUDA_TRY(cudaFree(r.stage_time));
         CUDA_TRY(cudaFree(r.orbit));
+        CUDA_TRY(cudaFree(r.stage_ds));
+        CUDA_TRY(cudaFree(r.stage_de));
         r.stage_time = nullptr;
         r.orbit = nullptr;
+        r.stage_ds = nullptr;
+        r.stage_de = nullptr;
         CUDA_TRY(cudaMalloc(&r.stage_time, sizeof(double) * cap));
         CUDA_TRY(cudaMalloc(&r.orbit, sizeof(double) * 10 * cap));
+        CUDA_TRY(cudaMalloc(&r.stage_ds, sizeof(double) * cap * r.nblocks * NITEMS * ctx->nf));
+        CUDA_TRY(cudaMalloc(&r.stage_de, sizeof(double) * cap * r.nblocks * 16));
         ctx->rdev_h[i].stage_time = r.stage_time;
         ctx->rdev_h[i].orbit = r.orbit;
+        ctx->rdev_h[i].stage_ds = r.stage_ds;
+        ctx->rdev_h[i].stage_de = r.stage_de;
     }
     ctx->max_stages = cap;
     CUDA_TRY(cudaMemcpy(ctx->rdev, ctx->rdev_h.data(), sizeof(RunDev) * ctx->nruns, cudaMemcpyHostToDevice));
@@ -702,7 +713,7 @@ extern "C" b2d_status b2d_max_signal_speed(b2d_ctx* ctx, int32_t run, double* ou
 // ---------------------------------------------------------------------------
 // The advance.
 
-static int free_slot(int a, int b, int c)
+__host__ __device__ static int free_slot(int a, int b, int c)
 {
     for (int s = 0; s < NSLOTS; ++s)
         if (s != a && s != b && s != c) return s;
@@ -737,6 +748,95 @@ static std::vector<StagePlan> plan_advance(int rk, int fold, int start, int* fin
     }
     *final_slot = base;
     return plan;
+}
+
+// ItemizedChange<OrbitalElements> of every block over one advance
+// (compute_block_updated_solution, scheme.rs:307-314), after the stage
+// kernels, which only record each block's stage sums ds·dx·dy: the serial
+// FP64 perturbation stays out of their tails.  Two launches:
+//  * elements_de_kernel — one thread per (stage, block, gas item sink1, sink2,
+//    grav1, grav2): that item's perturbation (ItemizedChange::perturbation,
+//    state.rs:258-281).  An unbound perturbed orbit fails its stage with
+//    OrbitalEvolutionError, reported at position (0, 0) as in the reference.
+//    The reference converts every block's primitives before it updates any
+//    block, so within a stage a cons->prim failure anywhere wins: the key's
+//    block field is saturated and the failing block's index rides in the
+//    zone field; an earlier stage still wins through the stage field.
+//  * elements_sum_kernel — one thread per (block, element component): the
+//    stages in order, e_out = e_in + de averaged like the state
+//    (state.rs:191-197), in the slot schedule of plan_advance.
+__global__ void elements_de_kernel(const RunDev* runs, int nstages, unsigned long long* err_key)
+{
+    const int run = blockIdx.z;
+    const RunDev& rd = runs[run];
+    const int s = blockIdx.y;
+    const int id = blockIdx.x * blockDim.x + threadIdx.x;   // block * 4 + item
+    if (s >= nstages || id >= rd.nblocks * 4 || !rd.stage_ds || !rd.stage_de) return;
+    const int block = id >> 2, item = id & 3;
+    const int nf = rd.p.hydro == B2D_EULER ? 4 : 3;
+    const double* ds = rd.stage_ds + ((size_t)s * rd.nblocks + block) * NITEMS * nf + item * nf;
+    const double* orbit = rd.orbit + 10 * s;
+    double* de = rd.stage_de + (((size_t)s * rd.nblocks + block) * 4 + item) * 4;
+    // pert1 (body 1: sink1, grav1) and pert2 (body 2: sink2, grav2), state.rs:261-269
+    const bool ok = (item == 0 || item == 2)
+                        ? perturb_elements(orbit, rd.el0, -ds[0], 0.0, -ds[1], 0.0, -ds[2], 0.0, de)
+                        : perturb_elements(orbit, rd.el0, 0.0, -ds[0], 0.0, -ds[1], 0.0, -ds[2], de);
+    if (!ok) {
+        de[0] = de[1] = de[2] = de[3] = 0.0;
+        const unsigned long long key = ((unsigned long long)s << 54) | ((unsigned long long)run << 46) |
+                                       (0xffffull << 30) | (0xfull << 26) | ((unsigned long long)block << 2) | 3ull;
+        atomicMin(err_key, key);
+    }
+}
+
+__global__ void elements_sum_kernel(const RunDev* runs, int fold, int rk, int start)
+{
+    const int run = blockIdx.y;
+    const RunDev& rd = runs[run];
+    const int id = blockIdx.x * blockDim.x + threadIdx.x;   // block * 28 + item * 4 + component
+    if (id >= rd.nblocks * NITEMS * 4 || !rd.stage_de || !rd.elements[start]) return;
+    const int block = id / (NITEMS * 4), k = id % (NITEMS * 4), item = k / 4;
+    double e[NSLOTS];
+    e[start] = rd.elements[start][id];
+    int s = 0;
+    auto stage = [&](int in, int base_slot, int out, double bf) {
+        const double de = item < 4 ? rd.stage_de[((size_t)s * rd.nblocks + block) * 16 + k] : 0.0;
+        double v = e[in] + de;
+        if (base_slot >= 0) v = v * (-bf + 1.0) + e[base_slot] * bf;
+        e[out] = v;
+        ++s;
+    };
+    // the schedule of plan_advance
+    int base = start;
+    for (int f = 0; f < fold; ++f) {
+        if (rk == 1) {
+            const int a = free_slot(start, base, -1);
+            stage(base, -1, a, 0.0);
+            base = a;
+        } else if (rk == 2) {
+            const int a = free_slot(start, base, -1);
+            stage(base, -1, a, 0.0);
+            const int b = free_slot(start, base, a);
+            stage(a, base, b, 0.5);
+            base = b;
+        } else {
+            const int a = free_slot(start, base, -1);
+            stage(base, -1, a, 0.0);
+            const int b = free_slot(start, base, a);
+            stage(a, base, b, 0.75);
+            const int c = free_slot(start, base, b);
+            stage(b, base, c, 1.0 / 3.0);
+            base = c;
+        }
+    }
+    rd.elements[base][id] = e[base];
+}
+
+static int max_blocks(const b2d_ctx* ctx)
+{
+    int m = 0;
+    for (const RunHost& r : ctx->runs) m = std::max(m, r.nblocks);
+    return m;
 }
 
 static df32w split_df(double v)
@@ -887,6 +987,14 @@ static b2d_status enqueue_advance(b2d_ctx* ctx, int fold, int start, int* final_
         st = launch_tracers(ctx, plan[s], count);
         if (st != B2D_OK) return st;
     }
+    const int nstages = (int)plan.size();
+    const dim3 dg((unsigned)((max_blocks(ctx) * 4 + 127) / 128), (unsigned)nstages, (unsigned)ctx->nruns);
+    elements_de_kernel<<<dg, 128, 0, ctx->stream>>>(ctx->rdev, nstages, ctx->d_err_key);
+    CUDA_TRY(cudaGetLastError());
+    const dim3 sg((unsigned)((max_blocks(ctx) * NITEMS * 4 + 127) / 128), (unsigned)ctx->nruns);
+    elements_sum_kernel<<<sg, 128, 0, ctx->stream>>>(ctx->rdev, fold, ctx->rk, start);
+    CUDA_TRY(cudaGetLastError());
+    if (count) ctx->launches += 2;
     return B2D_OK;
 }
 
@@ -1136,7 +1244,7 @@ extern "C" int64_t b2d_launches_per_advance(const b2d_ctx* ctx, int32_t fold)
     if (!ctx) return 0;
     int with_tracers = 0;
     for (const RunDev& d : ctx->rdev_h) with_tracers += d.ntracers > 0 ? 1 : 0;
-    return 1 + (int64_t)fold * ctx->rk * (1 + with_tracers);
+    return 3 + (int64_t)fold * ctx->rk * (1 + with_tracers);
 }
 
 extern "C" b2d_status b2d_set_instrument(b2d_ctx* ctx, int32_t enable)

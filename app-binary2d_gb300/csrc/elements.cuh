@@ -40,25 +40,4 @@ __host__ __device__ inline bool perturb_elements(const double* orbit, const doub
     return true;
 }
 
-// ItemizedChange<OrbitalElements> of one block from its stage sums ds·dx·dy
-// (items sink1, sink2, grav1, grav2, buffer, cooling, fake_mass; nf fields).
-// pert1 / pert2 (state.rs:261-269) take the negated mass and momentum of the
-// gas item; buffer, cooling and fake mass change nothing.  Returns false when
-// any perturbed orbit is unbound.
-__host__ __device__ inline bool block_perturbation(const double* orbit, const double* el, const double* ds, int nf,
-                                                   double* out /* [7][4] */)
-{
-    for (int k = 0; k < 28; ++k) out[k] = 0.0;
-    bool ok = true;
-    const double* s1 = ds + 0 * nf;
-    const double* s2 = ds + 1 * nf;
-    const double* g1 = ds + 2 * nf;
-    const double* g2 = ds + 3 * nf;
-    ok &= perturb_elements(orbit, el, -s1[0], 0.0, -s1[1], 0.0, -s1[2], 0.0, out + 0);
-    ok &= perturb_elements(orbit, el, 0.0, -s2[0], 0.0, -s2[1], 0.0, -s2[2], out + 4);
-    ok &= perturb_elements(orbit, el, -g1[0], 0.0, -g1[1], 0.0, -g1[2], 0.0, out + 8);
-    ok &= perturb_elements(orbit, el, 0.0, -g2[0], 0.0, -g2[1], 0.0, -g2[2], out + 12);
-    return ok;
-}
-
 }  // namespace b2d

@@ -72,16 +72,19 @@ template <> __device__ __forceinline__ float rsqrt_<float>(float a) { return sqr
 
 // ---------------------------------------------------------------------------
 // godunov-core piecewise_linear::plm_gradient (restated): generalised minmod
-// of θ(b - a), (c - a)/2, θ(c - b).
+// of θ(b - a), (c - a)/2, θ(c - b) — the smallest magnitude when all three
+// share a sign, else zero.  Written as max(min(x, y, z), 0) + min(max(x, y, z), 0):
+// with all three positive the first term is the minimum and the second 0,
+// with all negative the first is 0 and the second the maximum (the value of
+// smallest magnitude), with mixed signs (or a zero) both are 0.  min and max
+// round nothing, so this is the same value as the sign-test form, in four
+// min/max and one add instead of six compares and two selects.
 template <class R> __device__ __forceinline__ R plm_gradient(R th, R a, R b, R c)
 {
     R x = th * (b - a);
     R y = R(0.5) * (c - a);
     R z = th * (c - b);
-    bool pos = (x > R(0)) & (y > R(0)) & (z > R(0));
-    bool neg = (x < R(0)) & (y < R(0)) & (z < R(0));
-    R m = rmin(rabs(x), rmin(rabs(y), rabs(z)));
-    return pos ? m : (neg ? -m : R(0));
+    return rmax(rmin(rmin(x, y), z), R(0)) + rmin(rmax(rmax(x, y), z), R(0));
 }
 
 // ---------------------------------------------------------------------------
@@ -386,8 +389,12 @@ template <class R> __device__ __forceinline__ R buffer_rate(const DevParamsT<R>&
     }
 }
 
-template <int NF, class R>
-__device__ __forceinline__ void source_terms(const DevParamsT<R>& P, const Binary<R>& b, const R* u, const R* u0, R x, R y,
+// SPARSE (called by all 32 lanes of a warp together): the sink terms are
+// evaluated only when a zone of the warp lies inside a sink radius, and fake
+// mass only for a non-zero rate; otherwise those items are the zeros the full
+// formulas give.  Returns whether the sink items were evaluated.
+template <int NF, class R, bool SPARSE = false>
+__device__ __forceinline__ bool source_terms(const DevParamsT<R>& P, const Binary<R>& b, const R* u, const R* u0, R x, R y,
                                              R t, R dt, R* it /* [NITEMS][NF] */)
 {
     const R s2 = R(P.soft2);
@@ -396,21 +403,31 @@ __device__ __forceinline__ void source_terms(const DevParamsT<R>& P, const Binar
     point_acceleration(b.p2, x, y, s2, ax2, ay2);
     const R sigma = u[0];
     const R fx1 = sigma * ax1, fy1 = sigma * ay1, fx2 = sigma * ax2, fy2 = sigma * ay2;
-    const R sr1 = sink_kernel(P, x - b.p1.x, y - b.p1.y);
-    const R sr2 = sink_kernel(P, x - b.p2.x, y - b.p2.y);
+    bool sinks_on = true;
+    if constexpr (SPARSE) {
+        const R d1x = x - b.p1.x, d1y = y - b.p1.y, d2x = x - b.p2.x, d2y = y - b.p2.y;
+        const bool near = (d1x * d1x + d1y * d1y < R(P.sink_r2)) || (d2x * d2x + d2y * d2y < R(P.sink_r2));
+        sinks_on = __any_sync(0xffffffffu, near);
+    }
+    R sr1 = R(0), sr2 = R(0);
+    if (sinks_on) {
+        sr1 = sink_kernel(P, x - b.p1.x, y - b.p1.y);
+        sr2 = sink_kernel(P, x - b.p2.x, y - b.p2.y);
+    }
     const R br = buffer_rate(P, x, y);
     const R kb = -dt * br;
 
     if constexpr (NF == 3) {
         R fake[3];
-        if (u[0] < u0[0] * R(P.fake_thr)) {
+        if ((SPARSE && P.fake_rate == R(0)) || u[0] < u0[0] * R(P.fake_thr)) {
             fake[0] = fake[1] = fake[2] = R(0);
         } else {
 #pragma unroll
             for (int k = 0; k < 3; ++k) fake[k] = u0[k] * R(P.fake_rate) * dt;
         }
-        R s1[3], s2v[3];
-        if (P.sink_model == 0) {
+        R s1[3] = {R(0), R(0), R(0)}, s2v[3] = {R(0), R(0), R(0)};
+        if (!sinks_on) {
+        } else if (P.sink_model == 0) {
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
                 s1[k] = u[k] * -sr1;
@@ -483,8 +500,9 @@ __device__ __forceinline__ void source_terms(const DevParamsT<R>& P, const Binar
         R pc[4] = {p0[0], p0[1], p0[2], p0[0] * ec * R(P.gm1)};
         R uc[4];
         prim_to_cons<4, R>(P, pc, uc);
-        R s1[4], s2v[4];
-        if (P.sink_model == 0) {
+        R s1[4] = {R(0), R(0), R(0), R(0)}, s2v[4] = {R(0), R(0), R(0), R(0)};
+        if (!sinks_on) {
+        } else if (P.sink_model == 0) {
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 s1[k] = u[k] * -sr1;
@@ -517,6 +535,7 @@ __device__ __forceinline__ void source_terms(const DevParamsT<R>& P, const Binar
             it[FAKE_MASS * 4 + k] = R(0);
         }
     }
+    return sinks_on;
 }
 
 }  // namespace b2d

@@ -32,6 +32,8 @@ struct RunDev {
     unsigned long long* amax;
     double binary_q, binary_e;
     double* elements[NSLOTS];    // [nblocks][7][4] orbital-element change per slot (nullptr: not tracked)
+    double* stage_ds;            // [max_stages][nblocks][7 nf] block sums ds·dx·dy of each stage (nullptr: none)
+    double* stage_de;            // [max_stages][nblocks][4][4] element change of the gas items of each stage
     double el0[4];               // unperturbed elements (a, M, q, e), physics.rs:411-417
     long long ntracers;          // massless tracer particles of this run (0: none)
     double* tracers[NSLOTS];     // [ntracers][2] positions (x, y) per state slot

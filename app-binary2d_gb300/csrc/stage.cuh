@@ -17,7 +17,6 @@
 // __syncthreads per row orders all producer/consumer pairs.
 #pragma once
 
-#include "elements.cuh"
 #include "physics.cuh"
 #include "runtime.cuh"
 
@@ -130,37 +129,6 @@ __device__ __forceinline__ unsigned long long error_key(int stage, int run, cons
             best = k < best ? k : best;
         }
     return best;
-}
-
-// ItemizedChange<OrbitalElements> of one block for this stage
-// (compute_block_updated_solution, scheme.rs:307-314): the perturbation of
-// the block's stage sums ds·dx·dy, added to the input slot's value and
-// averaged like the state.  An unbound perturbed orbit fails the stage with
-// OrbitalEvolutionError, reported at block position (0, 0) as in the reference.
-template <int NF>
-__device__ __forceinline__ void finalize_elements(const StageArgs& a, const RunDev& rd, int ri, int block,
-                                                  const double* ds)
-{
-    if (!rd.elements[a.out_slot]) return;
-    double de[NITEMS * 4];
-    const bool ok = block_perturbation(rd.orbit + 10 * a.stage, rd.el0, ds, NF, de);
-    if (!ok) {
-        // The reference converts every block's primitives before it updates
-        // any block, so within a stage a cons->prim failure anywhere wins over
-        // an unbound orbit: the block field is saturated and the failing
-        // block's index rides in the zone field instead.
-        const unsigned long long key = ((unsigned long long)a.stage << 54) | ((unsigned long long)ri << 46) |
-                                       (0xffffull << 30) | (0xfull << 26) | ((unsigned long long)block << 2) | 3ull;
-        atomicMin(a.err_key, key);
-    }
-    const double* ein = rd.elements[a.in_slot] + (size_t)block * NITEMS * 4;
-    const double* ebase = a.base_slot >= 0 ? rd.elements[a.base_slot] + (size_t)block * NITEMS * 4 : nullptr;
-    double* eout = rd.elements[a.out_slot] + (size_t)block * NITEMS * 4;
-    for (int k = 0; k < NITEMS * 4; ++k) {
-        double v = __ldcg(ein + k) + de[k];
-        if (ebase) v = v * (-a.bf + 1.0) + __ldcg(ebase + k) * a.bf;
-        eout[k] = v;
-    }
 }
 
 // ----------------------------------------------------------------------------
@@ -416,23 +384,19 @@ __global__ void __launch_bounds__(256) stage_kernel(StageArgs a)
     __syncthreads();
     if (is_last) {
         __threadfence();
-        __shared__ double s_ds[NITEMS * 4];
         const double* lin = rd.ledger[a.in_slot] + (size_t)block * NL;
         const double* lbase = a.base_slot >= 0 ? rd.ledger[a.base_slot] + (size_t)block * NL : nullptr;
         double* lout = rd.ledger[a.out_slot] + (size_t)block * NL;
         for (int k = t; k < NL; k += TW) {
             double s = 0.0;
             for (int q = 0; q < rd.tiles_per_block; ++q) s += __ldcg(rd.partial + ((size_t)block * rd.tiles_per_block + q) * NL + k);
-            s_ds[k] = s * area;
             double v = __ldcg(lin + k) + s * area;
             if (lbase) v = v * (-a.bf + 1.0) + __ldcg(lbase + k) * a.bf;
             lout[k] = v;
+            // the block's ds·dx·dy of this stage, for the orbital-element ledger
+            if (rd.stage_ds) rd.stage_ds[((size_t)a.stage * rd.nblocks + block) * NL + k] = s * area;
         }
-        __syncthreads();
-        if (t == 0) {
-            finalize_elements<NF>(a, rd, ri, block, s_ds);
-            rd.counter[block] = 0u;
-        }
+        if (t == 0) rd.counter[block] = 0u;
     }
 }
 

@@ -49,27 +49,60 @@ __host__ __device__ inline int s2_smem_bytes(int nf, int store, int tw)
     return slots + exch + 8 * (S2_SLOTS + S2_USLOTS);
 }
 
+// Viscous stress, factored.  The face stress of stress_field (physics.rs:
+// 322-349) with the `nu` closure of scheme.rs:230-247 is
+//   tau_nn = (rho_l nu_l (s_nn,l + lambda bulk_l) + rho_r nu_r (s_nn,r + lambda bulk_r)) / 2
+// (and tau_t alike with s_xy and no bulk term).  nu_l = nu_r = nu for a
+// constant viscosity; for the alpha model nu_side = K(face) * cs2 with
+// K = alpha / Omega_2(face) / sqrt(gamma - 1), cs2 taken at the face from the
+// potential (isothermal, so nu_l = nu_r again) or from the cell's own
+// pressure (Euler).  Each cell therefore carries T_nn = c rho (s_nn + lambda
+// bulk) and T_xy = c rho s_xy with c = nu (constant), 1 (isothermal alpha) or
+// gamma p / rho (Euler alpha), and a face needs tau = K (T_l + T_r) / 2 with
+// K = 1 for the constant model: the stress algebra runs once per cell instead
+// of twice per face, and the alpha factor once per face instead of once per
+// side.  (This reassociates the FP32 stress; the FP64 kernels keep the
+// reference's order.)
 template <int NF>
-__device__ __forceinline__ float alpha_nu_f(const DevParamsF& P, const Binary<float>& b, float x, float y,
-                                            const float* pc)
+__device__ __forceinline__ float cell_visc_scale(const DevParamsF& P, const float* pc)
+{
+    if (P.visc == 0) return P.nu * pc[0];
+    if constexpr (NF == 3) return pc[0];
+    else return P.gamma * pc[3];
+}
+
+// K of the alpha model at a face (the cs2 of an isothermal face included).
+template <int NF>
+__device__ __forceinline__ float alpha_face_factor(const DevParamsF& P, const Binary<float>& b, float x, float y,
+                                                   float cs2_face)
 {
     float dx1 = x - b.p1.x, dy1 = y - b.p1.y, dx2 = x - b.p2.x, dy2 = y - b.p2.y;
     float a1 = sqrtf(dx1 * dx1 + dy1 * dy1) + P.eps_dx;
     float a2 = sqrtf(dx2 * dx2 + dy2 * dy2) + P.eps_dx;
-    float cs2;
-    if constexpr (NF == 3) cs2 = -binary_potential(b, x, y, P.soft2) * P.inv_mach2;
-    else cs2 = __fdividef(P.gamma * pc[3], pc[0]);
     float w2 = __fdividef(b.p1.m, a1 * a1 * a1) + __fdividef(b.p2.m, a2 * a2 * a2);
-    return P.nu * cs2 * rsqrtf(w2) * P.inv_sqrt_gm;
+    float k = P.nu * rsqrtf(w2) * P.inv_sqrt_gm;
+    if constexpr (NF == 3) k *= cs2_face;
+    return k;
+}
+
+// Isothermal face sound speed cs2 = -phi / M^2 (physics.rs:584-607) with the
+// Plummer potential phi = -sum_k m_k / sqrt(dx_k^2 + dy_k^2 + s^2): the x part
+// of each distance is shared by a tile row and the y part (with s^2) by a
+// column, so a face adds the two and takes one reciprocal root per body.
+__device__ __forceinline__ float iso_face_cs2(const DevParamsF& P, const Binary<float>& B, float dx1sq, float dx2sq,
+                                              float cy1, float cy2)
+{
+    return (B.p1.m * rsqrtf(dx1sq + cy1) + B.p2.m * rsqrtf(dx2sq + cy2)) * P.inv_mach2;
 }
 
 // intercell_flux (physics.rs:584-607 iso, 776-803 euler) from the two cells'
-// primitive (pc), slope along the face normal (g) and stress terms: sn the
-// normal-normal shear term, st the off-diagonal one, bk the bulk term.
+// primitive (pc), slope along the face normal (g) and factored stresses (tn:
+// normal-normal, tt: off-diagonal); cs2 is the isothermal face sound speed
+// (unused for Euler).
 template <int NF, int AXIS>
 __device__ __forceinline__ void face_flux(const DevParamsF& P, const Binary<float>& B, const float* pcl,
-                                          const float* gl, float snl, float stl, float bkl, const float* pcr,
-                                          const float* gr, float snr, float str, float bkr, float x, float y,
+                                          const float* gl, float tnl, float ttl, const float* pcr,
+                                          const float* gr, float tnr, float ttr, float x, float y, float cs2,
                                           float* F)
 {
     float pl[NF], pr[NF];
@@ -78,20 +111,11 @@ __device__ __forceinline__ void face_flux(const DevParamsF& P, const Binary<floa
         pl[k] = pcl[k] + 0.5f * gl[k];
         pr[k] = pcr[k] - 0.5f * gr[k];
     }
-    float lnu, rnu;
-    if (P.visc == 0) {
-        lnu = rnu = P.nu;
-    } else {
-        lnu = alpha_nu_f<NF>(P, B, x, y, pcl);
-        rnu = alpha_nu_f<NF>(P, B, x, y, pcr);
-    }
-    const float lam = P.lambda;
-    const float tn = 0.5f * (pcl[0] * (lnu * snl + lam * lnu * bkl) + pcr[0] * (rnu * snr + lam * rnu * bkr));
-    const float tt = 0.5f * (pcl[0] * (lnu * stl) + pcr[0] * (rnu * str));
+    const float k = P.visc == 0 ? 0.5f : 0.5f * alpha_face_factor<NF>(P, B, x, y, cs2);
+    const float tn = k * (tnl + tnr);
+    const float tt = k * (ttl + ttr);
     const float tau_x = AXIS == 0 ? tn : tt;
     const float tau_y = AXIS == 0 ? tt : tn;
-    float cs2 = 0.0f;
-    if constexpr (NF == 3) cs2 = -binary_potential(B, x, y, P.soft2) * P.inv_mach2;
     hlle<NF, float>(P, pl, pr, AXIS, cs2, F);
     F[1] -= tau_x;
     F[2] -= tau_y;
@@ -117,6 +141,29 @@ template <int NF> __host__ __device__ constexpr int live_items()
         bool dead = ((item == GRAV1 || item == GRAV2) && f == 0) || (NF == 3 && item == COOLING) ||
                     (NF == 4 && item == FAKE_MASS);
         n += dead ? 0 : 1;
+    }
+    return n;
+}
+
+// Reduction groups of the live items: 0 = gravity, buffer and cooling (non-zero
+// almost everywhere), 1 = the two sinks (zero outside the sink radii), 2 =
+// fake mass (zero unless a fake-mass rate is set).  A warp reduces group 1
+// only when one of its zones lies inside a sink, and group 2 only for a
+// non-zero rate: the sums are the same, since the skipped terms are zeros.
+template <int NF> __host__ __device__ constexpr int item_group(int k)
+{
+    const int item = k / NF;
+    return (item == SINK1 || item == SINK2) ? 1 : (item == FAKE_MASS ? 2 : 0);
+}
+
+template <int NF, int G> __host__ __device__ constexpr int group_size()
+{
+    int n = 0;
+    for (int k = 0; k < NITEMS * NF; ++k) {
+        const int item = k / NF, f = k % NF;
+        bool dead = ((item == GRAV1 || item == GRAV2) && f == 0) || (NF == 3 && item == COOLING) ||
+                    (NF == 4 && item == FAKE_MASS);
+        n += (!dead && item_group<NF>(k) == G) ? 1 : 0;
     }
     return n;
 }
@@ -157,6 +204,45 @@ template <int K> __device__ __forceinline__ int item_of_lane(int lane)
     return item;
 }
 
+// The per-warp ledger slot (index among the live items) that `lane` adds its
+// warp_sum_items result of group G to, or -1.
+template <int NF, int G> __device__ __forceinline__ int group_writer_slot(int lane)
+{
+    constexpr int NG = group_size<NF, G>();
+    constexpr int KG = pow2_at_least<NG>();
+    if (NG == 0 || (lane & (32 / KG - 1)) != 0) return -1;
+    const int m = item_of_lane<KG>(lane);
+    if (m >= NG) return -1;
+    int live = 0, member = 0;
+    for (int k = 0; k < NITEMS * NF; ++k) {
+        if (!item_live<NF>(k)) continue;
+        if (item_group<NF>(k) == G) {
+            if (member == m) return live;
+            ++member;
+        }
+        ++live;
+    }
+    return -1;
+}
+
+// Warp-sum the live items of group G of this zone's `it` and add them to the
+// warp's ledger slots.
+template <int NF, int G>
+__device__ __forceinline__ void reduce_group(const float* it, int lane, int slot, float* led)
+{
+    constexpr int NG = group_size<NF, G>();
+    constexpr int KG = pow2_at_least<NG>();
+    float v[KG];
+    int j = 0;
+#pragma unroll
+    for (int k = 0; k < NITEMS * NF; ++k)
+        if (item_live<NF>(k) && item_group<NF>(k) == G) v[j++] = it[k];
+#pragma unroll
+    for (int k = NG; k < KG; ++k) v[k] = 0.0f;
+    const float s = warp_sum_items<KG>(v, lane);
+    if (slot >= 0) led[slot] += s;
+}
+
 template <bool SINGLE>
 __device__ __forceinline__ const DevParamsF& params_for(const StageArgs& a, const DevParamsF& shared_copy)
 {
@@ -169,6 +255,7 @@ __global__ void __launch_bounds__(160, (NF == 3 && STORE == 1) ? 4 : 3) stage2_k
 {
     using E = typename std::conditional<STORE == 1, float, double>::type;
     constexpr int H = STORE == 1 ? 4 : 2;     // staged halo columns per side: 16 bytes
+    constexpr int RQ = (2 * NF + 2 + 3) / 4;  // float4 planes of a y-face record
     constexpr int NL = NITEMS * NF;
 
     const int TW = blockDim.x - 32;
@@ -318,23 +405,34 @@ __global__ void __launch_bounds__(160, (NF == 3 && STORE == 1) ? 4 : 3) stage2_k
     const float yv_own = has_fy ? xv[bj * (bs + 1) + lj0 + c] : 0.0f;
     const float* xv_row = xv + bi * (bs + 1) + li0;    // x of face (i0 + r) - 1/2 is xv_row[r]
     const float* xc_row = xc + i0;
+    // column parts (dy^2 + s^2) of the body distances of this column's faces
+    float cyv1 = 0.0f, cyv2 = 0.0f, cyc1 = 0.0f, cyc2 = 0.0f;
+    if constexpr (NF == 3) {
+        const float dv1 = yv_own - B.p1.y, dv2 = yv_own - B.p2.y, dc1 = yc_own - B.p1.y, dc2 = yc_own - B.p2.y;
+        cyv1 = dv1 * dv1 + P.soft2;
+        cyv2 = dv2 * dv2 + P.soft2;
+        cyc1 = dc1 * dc1 + P.soft2;
+        cyc2 = dc2 * dc2 + P.soft2;
+    }
 
     float Pm1[NF], P0[NF];               // primitives of rows rg-1, rg (own column)
-    float rxa[2 * NF + 3], rxb[2 * NF + 3];  // x-face records of rows rq, rq+1: pc, gx, sxx, sxy, bulk
+    float rxa[2 * NF + 2], rxb[2 * NF + 2];  // x-face records of rows rq, rq+1: pc, gx, txx, txy
     float fxA[NF], fxB[NF];              // x fluxes at faces ru-1/2, ru+1/2
     // source ledger: per-warp accumulators of the live items, one lane each
     constexpr int NLIVE = live_items<NF>();
-    constexpr int KL = pow2_at_least<NLIVE>();
+    static_assert(group_size<NF, 0>() + group_size<NF, 1>() + group_size<NF, 2>() == NLIVE, "ledger groups");
     __shared__ float sLed[4][32];
     const int lane = t & 31, warp = t >> 5;
     if (t < 128) sLed[t >> 5][t & 31] = 0.0f;
-    const int my_item = item_of_lane<KL>(lane);
-    const bool item_writer = my_item < NLIVE && (lane & (32 / KL - 1)) == 0;
+    const int slot0 = group_writer_slot<NF, 0>(lane);
+    const int slot1 = group_writer_slot<NF, 1>(lane);
+    const int slot2 = group_writer_slot<NF, 2>(lane);
+    const bool fake_on = group_size<NF, 2>() > 0 && P.fake_rate != 0.0f;
     float amax = 0.0f;
 #pragma unroll
     for (int f = 0; f < NF; ++f) { Pm1[f] = P0[f] = fxA[f] = fxB[f] = 0.0f; }
 #pragma unroll
-    for (int w = 0; w < 2 * NF + 3; ++w) rxa[w] = rxb[w] = 0.0f;
+    for (int w = 0; w < 2 * NF + 2; ++w) rxa[w] = rxb[w] = 0.0f;
 
     for (int k = 0; k < TH + 5; ++k) {
         const int rn = k - 2;
@@ -379,32 +477,32 @@ __global__ void __launch_bounds__(160, (NF == 3 && STORE == 1) ? 4 : 3) stage2_k
                 gx[f] = plm_gradient(thx, Pm1[f], P0[f], pn[f]);
                 gy[f] = plm_gradient(thy, lv[f], P0[f], rv[f]);
             }
+            // stress_field terms (physics.rs:322-340), factored per cell (see face_flux)
             const float da = gx[1] * inv_dx, db = gy[2] * inv_dx;
-            const float sxx = (4.0f / 3.0f) * da - (2.0f / 3.0f) * db;
-            const float syy = (4.0f / 3.0f) * db - (2.0f / 3.0f) * da;
-            const float sxy = (gx[2] + gy[1]) * inv_dx;
-            const float bulk = da + db;
-            // y-face record for the right neighbour: pc | gy | sxy, syy, bulk
-            float yr[12];
+            const float lb = P.lambda * (da + db);
+            const float cv = cell_visc_scale<NF>(P, P0);
+            const float txx = cv * ((4.0f / 3.0f) * da - (2.0f / 3.0f) * db + lb);
+            const float tyy = cv * ((4.0f / 3.0f) * db - (2.0f / 3.0f) * da + lb);
+            const float txy = cv * ((gx[2] + gy[1]) * inv_dx);
+            // y-face record for the right neighbour: pc | gy | tyy, txy
+            float yr[4 * RQ];
 #pragma unroll
             for (int f = 0; f < NF; ++f) { yr[f] = P0[f]; yr[NF + f] = gy[f]; }
-            yr[2 * NF] = sxy;
-            yr[2 * NF + 1] = syy;
-            yr[2 * NF + 2] = bulk;
+            yr[2 * NF] = tyy;
+            yr[2 * NF + 1] = txy;
 #pragma unroll
-            for (int w = 2 * NF + 3; w < 12; ++w) yr[w] = 0.0f;
+            for (int w = 2 * NF + 2; w < 4 * RQ; ++w) yr[w] = 0.0f;
             const int o = (rg & 1) * (TW + 2) + c + 1;
             sR0[o] = make_float4(yr[0], yr[1], yr[2], yr[3]);
             sR1[o] = make_float4(yr[4], yr[5], yr[6], yr[7]);
-            sR2[o] = make_float4(yr[8], yr[9], yr[10], yr[11]);
+            if constexpr (RQ == 3) sR2[o] = make_float4(yr[8], yr[9], yr[10], yr[11]);
             // x-face record kept in registers
 #pragma unroll
-            for (int w = 0; w < 2 * NF + 3; ++w) rxa[w] = rxb[w];
+            for (int w = 0; w < 2 * NF + 2; ++w) rxa[w] = rxb[w];
 #pragma unroll
             for (int f = 0; f < NF; ++f) { rxb[f] = P0[f]; rxb[NF + f] = gx[f]; }
-            rxb[2 * NF] = sxx;
-            rxb[2 * NF + 1] = sxy;
-            rxb[2 * NF + 2] = bulk;
+            rxb[2 * NF] = txx;
+            rxb[2 * NF + 1] = txy;
         }
         if (rn <= TH + 1) {
 #pragma unroll
@@ -424,14 +522,19 @@ __global__ void __launch_bounds__(160, (NF == 3 && STORE == 1) ? 4 : 3) stage2_k
         const bool up_ok = ru >= 0 && ru <= TH - 1;
         auto y_flux = [&]() {
             const int ol = (rq & 1) * (TW + 2) + c, orr = ol + 1;
-            const float4 v0 = sR0[ol], v1 = sR1[ol], v2 = sR2[ol];
-            const float4 w0 = sR0[orr], w1v = sR1[orr], w2 = sR2[orr];
+            const float4 v0 = sR0[ol], v1 = sR1[ol], v2 = RQ == 3 ? sR2[ol] : make_float4(0.f, 0.f, 0.f, 0.f);
+            const float4 w0 = sR0[orr], w1v = sR1[orr], w2 = RQ == 3 ? sR2[orr] : make_float4(0.f, 0.f, 0.f, 0.f);
             const float L[12] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w, v2.x, v2.y, v2.z, v2.w};
             const float Rr[12] = {w0.x, w0.y, w0.z, w0.w, w1v.x, w1v.y, w1v.z, w1v.w, w2.x, w2.y, w2.z, w2.w};
             const float x = xc_row[min(max(rq, 0), TH - 1)];
+            float cs2 = 0.0f;
+            if constexpr (NF == 3) {
+                const float d1 = x - B.p1.x, d2 = x - B.p2.x;
+                cs2 = iso_face_cs2(P, B, d1 * d1, d2 * d2, cyv1, cyv2);
+            }
             float F[NF];
-            face_flux<NF, 1>(P, B, L, L + NF, L[2 * NF + 1], L[2 * NF], L[2 * NF + 2], Rr, Rr + NF, Rr[2 * NF + 1],
-                             Rr[2 * NF], Rr[2 * NF + 2], x, yv_own, F);
+            face_flux<NF, 1>(P, B, L, L + NF, L[2 * NF], L[2 * NF + 1], Rr, Rr + NF, Rr[2 * NF], Rr[2 * NF + 1], x,
+                             yv_own, cs2, F);
             if (fy_ok) sF[(rq & 1) * (TW + 1) + c] = make_float4(F[0], F[1], F[2], NF == 4 ? F[NF - 1] : 0.0f);
         };
         float fxn[NF];
@@ -454,14 +557,27 @@ __global__ void __launch_bounds__(160, (NF == 3 && STORE == 1) ? 4 : 3) stage2_k
                     u0[f] = STORE == 1 ? (float)q[(NF + f) * TW + c] : (float)q[f * TW + c];
                 }
                 float it[NL];
-                source_terms<NF, float>(P, B, uc, u0, x, yc_own, time, dt, it);
+                const bool sinks_on = source_terms<NF, float, true>(P, B, uc, u0, x, yc_own, time, dt, it);
+                // the items' total, leaving out the ones that are zero for the whole warp
+                float tot[NF];
+#pragma unroll
+                for (int f = 0; f < NF; ++f) {
+                    tot[f] = it[GRAV1 * NF + f] + it[GRAV2 * NF + f] + it[BUFFER * NF + f];
+                    if constexpr (NF == 4) tot[f] += it[COOLING * NF + f];
+                }
+                if (sinks_on) {
+#pragma unroll
+                    for (int f = 0; f < NF; ++f) tot[f] += it[SINK1 * NF + f] + it[SINK2 * NF + f];
+                }
+                if (NF == 3 && fake_on) {
+#pragma unroll
+                    for (int f = 0; f < NF; ++f) tot[f] += it[FAKE_MASS * NF + f];
+                }
                 const size_t idx = (size_t)(i0 + rc) * N + (j0 + c);
 #pragma unroll
                 for (int f = 0; f < NF; ++f) {
-                    float tot = it[SINK1 * NF + f] + it[SINK2 * NF + f] + it[GRAV1 * NF + f] + it[GRAV2 * NF + f] +
-                                it[BUFFER * NF + f] + it[COOLING * NF + f] + it[FAKE_MASS * NF + f];
                     float du = ((fxB[f] - fxA[f]) + (fyr[f] - fyl[f])) * inv_dx * -dt;
-                    float inc = du + tot;
+                    float inc = du + tot[f];
                     if constexpr (STORE == 1) {
                         df32 o = df_add_f(df32{(float)sb[f * SW + c + H], (float)q[f * TW + c]}, inc);
                         if (has_base) {
@@ -486,23 +602,24 @@ __global__ void __launch_bounds__(160, (NF == 3 && STORE == 1) ? 4 : 3) stage2_k
                     }
                 }
                 if (up_ok) {   // the same row for the whole warp
-                    float v[KL];
-                    int j = 0;
-#pragma unroll
-                    for (int k2 = 0; k2 < NL; ++k2)
-                        if (item_live<NF>(k2)) v[j++] = it[k2];
-#pragma unroll
-                    for (int k2 = NLIVE; k2 < KL; ++k2) v[k2] = 0.0f;
-                    const float s = warp_sum_items<KL>(v, lane);
-                    if (item_writer) sLed[warp][my_item] += s;
+                    reduce_group<NF, 0>(it, lane, slot0, sLed[warp]);
+                    if (sinks_on) reduce_group<NF, 1>(it, lane, slot1, sLed[warp]);
+                    if (fake_on) reduce_group<NF, 2>(it, lane, slot2, sLed[warp]);
                 }
                 if (want_amax && up_ok) amax = fmaxf(max_signal_speed<NF, float>(P, uc), amax);
             }
 
             // x flux of face rq + 1/2
-            face_flux<NF, 0>(P, B, rxa, rxa + NF, rxa[2 * NF], rxa[2 * NF + 1], rxa[2 * NF + 2], rxb, rxb + NF,
-                             rxb[2 * NF], rxb[2 * NF + 1], rxb[2 * NF + 2], xv_row[min(max(rq + 1, 0), TH)], yc_own,
-                             fxn);
+            {
+                const float x = xv_row[min(max(rq + 1, 0), TH)];
+                float cs2 = 0.0f;
+                if constexpr (NF == 3) {
+                    const float d1 = x - B.p1.x, d2 = x - B.p2.x;
+                    cs2 = iso_face_cs2(P, B, d1 * d1, d2 * d2, cyc1, cyc2);
+                }
+                face_flux<NF, 0>(P, B, rxa, rxa + NF, rxa[2 * NF], rxa[2 * NF + 1], rxb, rxb + NF, rxb[2 * NF],
+                                 rxb[2 * NF + 1], x, yc_own, cs2, fxn);
+            }
         } else if (hl == 2 && fy_ok) {
             y_flux();
         }
@@ -553,21 +670,17 @@ __global__ void __launch_bounds__(160, (NF == 3 && STORE == 1) ? 4 : 3) stage2_k
         const double* lin = rd.ledger[a.in_slot] + (size_t)block * NL;
         const double* lbase = has_base ? rd.ledger[a.base_slot] + (size_t)block * NL : nullptr;
         double* lout = rd.ledger[a.out_slot] + (size_t)block * NL;
-        __shared__ double s_ds[NITEMS * 4];
         for (int k = t; k < NL; k += NT) {
             double s = 0.0;
             for (int q = 0; q < rd.tiles_per_block; ++q)
                 s += __ldcg(rd.partial + ((size_t)block * rd.tiles_per_block + q) * NL + k);
-            s_ds[k] = s * area;
             double v = __ldcg(lin + k) + s * area;
             if (lbase) v = v * (-a.bf + 1.0) + __ldcg(lbase + k) * a.bf;
             lout[k] = v;
+            // the block's ds·dx·dy of this stage, for the orbital-element ledger
+            if (rd.stage_ds) rd.stage_ds[((size_t)a.stage * rd.nblocks + block) * NL + k] = s * area;
         }
-        __syncthreads();
-        if (t == 0) {
-            finalize_elements<NF>(a, rd, ri, block, s_ds);
-            rd.counter[block] = 0u;
-        }
+        if (t == 0) rd.counter[block] = 0u;
     }
 }
 

@@ -1,0 +1,129 @@
+"""One-orbit accuracy of the three precisions on the 2048² isothermal disk,
+against the CPU oracle.
+
+Two steps, because the oracle's orbit costs about 8e10 zone-updates:
+
+    python tests/orbit_accuracy.py oracle --out tests/_cache/orbit2048.npz [--threads N]
+    python tests/orbit_accuracy.py gpu --cache tests/_cache/orbit2048.npz [--json OUT]
+
+The first runs the oracle for one orbit (fold 10 advances until t >= 2π) and
+caches Σ at the end and the time series of the domain totals of the
+ItemizedChange ledger (state.rs:27-62) and of the orbital-element ledger
+after every advance (TimeSeriesSample, app.rs:141-148).  The second runs the
+same number of advances on the GPU in every precision and reports the
+relative L1 error of Σ and the error of each ledger series against the
+cached oracle run.  The cache is a regenerable test artefact and is not
+committed.
+"""
+import argparse
+import json
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+sys.path.insert(0, os.path.join(ROOT, "app-binary2d_gb300"))
+sys.path.insert(0, ROOT)
+
+FOLD = 10
+ITEMS = ("sink1", "sink2", "grav1", "grav2", "buffer", "cooling", "fake_mass")
+
+
+def _case(side):
+    import binary2d as b2
+    if side == 2048:
+        mesh, hydro, physics, model = b2.presets.disk_2048(seed=1)
+    else:
+        mesh, hydro, physics, model = b2.presets.iso_disk(side // 64, 64, seed=1)
+    cons = b2.initial_state(mesh, hydro, physics, model)
+    return mesh, hydro, physics, cons
+
+
+def run_oracle(args):
+    import binary2d as b2
+    from oracle import binding
+    mesh, hydro, physics, cons = _case(args.side)
+    st = binding.OracleState(b2.to_c(mesh, hydro, physics), cons)
+    t_end = args.orbits * 2 * np.pi
+    times, led, el, dts = [], [], [], []
+    t0 = time.time()
+    while st.time.value < t_end:
+        dts.append(st.advance(FOLD, nthreads=args.threads))
+        times.append(st.time.value)
+        led.append(st.ledger.sum(axis=(0, 1)))
+        el.append(st.elements.sum(axis=(0, 1)))
+        if len(times) % 50 == 0:
+            print("advance %d t=%.4f (%.0f s)" % (len(times), st.time.value, time.time() - t0), flush=True)
+    os.makedirs(os.path.dirname(os.path.abspath(args.out)), exist_ok=True)
+    np.savez(args.out, sigma=st.cons[..., 0], times=np.array(times), ledger=np.array(led),
+             elements=np.array(el), dts=np.array(dts), side=args.side, orbits=args.orbits,
+             seconds=time.time() - t0)
+    print("wrote %s: %d advances, t=%.6f, %.0f s" % (args.out, len(times), st.time.value, time.time() - t0))
+
+
+def run_gpu(args):
+    import binary2d as b2
+    ref = np.load(args.cache)
+    side = int(ref["side"])
+    mesh, hydro, physics, cons = _case(side)
+    n = len(ref["times"])
+    sig_ref = ref["sigma"]
+    out = {"workload": "iso disk %d^2, one orbit" % side, "advances": n, "steps": n * FOLD,
+           "orbits": float(ref["times"][-1] / (2 * np.pi)),
+           "oracle_seconds": float(ref["seconds"]), "precisions": {}}
+    for p in ("fp64", "fp32_state64", "fp32_comp"):
+        with b2.Runtime([b2.Run(mesh, hydro, physics)], precision=p) as rt:
+            rt.autotune()
+            rt.upload(0, cons)
+            times, led, el = [], [], []
+            t0 = time.time()
+            for _ in range(n):
+                rt.advance(FOLD)
+                times.append(rt.time(0)[0])
+                led.append(rt.ledger(0).sum(axis=(0, 1)))
+                el.append(rt.elements(0).sum(axis=(0, 1)))
+            secs = time.time() - t0
+            s, t, _ = rt.download(0)
+        led, el = np.array(led), np.array(el)
+        l1 = float(np.abs(s[..., 0] - sig_ref).sum() / np.abs(sig_ref).sum())
+        # per item and field: max over the series of |gpu - oracle| / max |oracle|
+        scale = np.maximum(np.abs(ref["ledger"]).max(axis=0), 1e-300)
+        led_err = (np.abs(led - ref["ledger"]).max(axis=0) / scale)
+        escale = np.maximum(np.abs(ref["elements"]).max(axis=0), 1e-300)
+        el_err = (np.abs(el - ref["elements"]).max(axis=0) / escale)
+        acc = ref["ledger"][-1, 0:2, 0].sum()
+        out["precisions"][p] = {
+            "l1_sigma_rel": l1,
+            "end_time_rel": float(abs(t - ref["times"][-1]) / ref["times"][-1]),
+            "accreted_mass_rel": float(abs(led[-1, 0:2, 0].sum() - acc) / abs(acc)),
+            "ledger_series_rel": {ITEMS[k]: float(led_err[k].max()) for k in range(7) if np.abs(ref["ledger"][:, k]).max() > 0},
+            "elements_series_rel": {ITEMS[k]: float(el_err[k].max()) for k in range(4)},
+            "seconds_with_host_sampling": secs,
+        }
+        print(p, json.dumps(out["precisions"][p]), flush=True)
+    if args.json:
+        with open(args.json, "w") as f:
+            json.dump(out, f, indent=1)
+    print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    sub = ap.add_subparsers(dest="cmd", required=True)
+    o = sub.add_parser("oracle")
+    o.add_argument("--out", required=True)
+    o.add_argument("--side", type=int, default=2048)
+    o.add_argument("--orbits", type=float, default=1.0)
+    o.add_argument("--threads", type=int, default=None)
+    g = sub.add_parser("gpu")
+    g.add_argument("--cache", required=True)
+    g.add_argument("--json", default="")
+    args = ap.parse_args()
+    run_oracle(args) if args.cmd == "oracle" else run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()
