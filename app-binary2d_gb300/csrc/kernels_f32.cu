@@ -1,9 +1,11 @@
 // kernels_f32.cu — FP32-stencil stage kernels over FP64 state (store 0) or
-// compensated FP32 state (store 1).  Tiles whose width is a multiple of 32
-// run the TMA-staged kernel of stage2.cuh; narrower tiles (blocks of fewer
-// than 32 zones) run the generic kernel of stage.cuh.
+// compensated FP32 state (store 1).  Isothermal compensated tiles whose width
+// is a multiple of 64 run the paired-column kernel of stage3.cuh; other tiles
+// whose width is a multiple of 32 run the TMA-staged kernel of stage2.cuh;
+// narrower tiles (blocks of fewer than 32 zones) run the generic kernel of
+// stage.cuh.
 #include "kernels.inc"
-#include "stage2.cuh"
+#include "stage3.cuh"
 
 namespace b2d {
 
@@ -31,8 +33,25 @@ static cudaError_t launch_two(const StageArgs& a, int grid, int tw, cudaStream_t
     return launch_two_impl<NF, STORE, false>(a, grid, tw, s);
 }
 
+template <bool SINGLE>
+static cudaError_t launch_three_impl(const StageArgs& a, int grid, int tw, cudaStream_t s)
+{
+    auto k = stage3_kernel<SINGLE>;
+    size_t smem = s3_smem_bytes(tw);
+    static size_t configured = 0;
+    if (smem > configured) {
+        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        configured = smem;
+    }
+    k<<<grid, tw / 2 + 32, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_stage_f32(int nf, int store, const StageArgs& a, int grid, int tw, size_t smem, cudaStream_t s)
 {
+    if (nf == 3 && store == 1 && tw % 64 == 0 && tw <= 128)
+        return a.nruns == 1 ? launch_three_impl<true>(a, grid, tw, s) : launch_three_impl<false>(a, grid, tw, s);
     if (tw % 32 == 0 && tw <= 128) {
         if (nf == 3) return store == 0 ? launch_two<3, 0>(a, grid, tw, s) : launch_two<3, 1>(a, grid, tw, s);
         return store == 0 ? launch_two<4, 0>(a, grid, tw, s) : launch_two<4, 1>(a, grid, tw, s);
