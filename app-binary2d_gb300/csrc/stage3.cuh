@@ -441,46 +441,81 @@ __global__ void __launch_bounds__(96, 4) stage3_kernel(StageArgs a)
                     ulo[f] = *(const float2*)(q + f * TW + c0);
                     u0[f] = *(const float2*)(q + (NF + f) * TW + c0);
                 }
-                // sources of each column (Physics::source_terms, physics.rs:423-457, 528-582)
-                float it[NL];
+                // sources of the pair (Physics::source_terms, physics.rs:423-457;
+                // Isothermal::source_terms, physics.rs:528-582): gravity and the
+                // buffer packed; sinks (a warp with a zone inside a sink radius)
+                // and fake mass (a non-zero rate) per column
                 float2 tot[NF];
                 float led0[8], led1[8], led2[4];
+                bool sinks_any;
+                {
+                    const float dx1 = x - B.p1.x, dx2 = x - B.p2.x;
+                    const float2 dy1 = sub2(yc2, f2(B.p1.y)), dy2 = sub2(yc2, f2(B.p2.y));
+                    // Plummer accelerations (kepler-two-body, restated): -m d / (d^2 + s^2)^(3/2)
+                    const float2 t1 = fma2(dy1, dy1, f2(fmaf(dx1, dx1, P.soft2)));
+                    const float2 t2 = fma2(dy2, dy2, f2(fmaf(dx2, dx2, P.soft2)));
+                    const float2 r1 = make_float2(rsqrtf(t1.x), rsqrtf(t1.y));
+                    const float2 r2 = make_float2(rsqrtf(t2.x), rsqrtf(t2.y));
+                    const float2 sdt = mul2(uc[0], f2(dt));
+                    const float2 q1 = mul2(mul2(sdt, f2(-B.p1.m)), mul2(r1, mul2(r1, r1)));
+                    const float2 q2 = mul2(mul2(sdt, f2(-B.p2.m)), mul2(r2, mul2(r2, r2)));
+                    const float2 g1x = mul2(q1, f2(dx1)), g1y = mul2(q1, dy1);
+                    const float2 g2x = mul2(q2, f2(dx2)), g2y = mul2(q2, dy2);
+                    // buffer: 0.5 rate (1 + tanh((r - R) / scale)) Omega_outer, 1 + tanh(y) = 2 / (1 + exp(-2y))
+                    const float2 rr2 = fma2(yc2, yc2, f2(x * x));
+                    const float2 yb = mul2(sub2(make_float2(sqrtf(rr2.x), sqrtf(rr2.y)), f2(P.domain_radius)),
+                                           f2(-2.0f * P.inv_buffer_scale));
+                    const float2 den = add2(f2(1.0f), make_float2(__expf(yb.x), __expf(yb.y)));
+                    const float2 kb = mul2(f2(-2.0f * dt * P.half_rate_omega),
+                                           make_float2(__fdividef(1.0f, den.x), __fdividef(1.0f, den.y)));
+                    float2 bu[NF];
 #pragma unroll
-                for (int m = 0; m < 8; ++m) led0[m] = led1[m] = 0.0f;
+                    for (int f = 0; f < NF; ++f) bu[f] = mul2(sub2(uc[f], u0[f]), kb);
+                    tot[0] = bu[0];
+                    tot[1] = add2(add2(g1x, g2x), bu[1]);
+                    tot[2] = add2(add2(g1y, g2y), bu[2]);
+                    // ledger group 0 in item order: grav1 (x, y), grav2 (x, y), buffer (3 fields)
+                    led0[0] = g1x.x + g1x.y; led0[1] = g1y.x + g1y.y;
+                    led0[2] = g2x.x + g2x.y; led0[3] = g2y.x + g2y.y;
+                    led0[4] = bu[0].x + bu[0].y; led0[5] = bu[1].x + bu[1].y; led0[6] = bu[2].x + bu[2].y;
+                    led0[7] = 0.0f;
 #pragma unroll
-                for (int m = 0; m < 4; ++m) led2[m] = 0.0f;
-                bool sinks_any = false;
+                    for (int m = 0; m < 8; ++m) led1[m] = 0.0f;
 #pragma unroll
-                for (int side = 0; side < 2; ++side) {
-                    const float us[NF] = {side ? uc[0].y : uc[0].x, side ? uc[1].y : uc[1].x, side ? uc[2].y : uc[2].x};
-                    const float u0s[NF] = {side ? u0[0].y : u0[0].x, side ? u0[1].y : u0[1].x,
-                                           side ? u0[2].y : u0[2].x};
-                    const bool sinks_on = source_terms<NF, float, true>(P, B, us, u0s, x, side ? yc2.y : yc2.x, time, dt, it);
-                    sinks_any = sinks_any || sinks_on;
-                    float ts[NF];
+                    for (int m = 0; m < 4; ++m) led2[m] = 0.0f;
+                    // sinks: only where a zone of the warp lies inside a sink radius
+                    const float2 s1 = fma2(dy1, dy1, f2(dx1 * dx1)), s2 = fma2(dy2, dy2, f2(dx2 * dx2));
+                    const bool near = s1.x < P.sink_r2 || s1.y < P.sink_r2 || s2.x < P.sink_r2 || s2.y < P.sink_r2;
+                    sinks_any = __any_sync(0xffffffffu, near);
+                    if (sinks_any) {
+                        float it[NL];
 #pragma unroll
-                    for (int f = 0; f < NF; ++f) ts[f] = it[GRAV1 * NF + f] + it[GRAV2 * NF + f] + it[BUFFER * NF + f];
-                    if (sinks_on) {
+                        for (int side = 0; side < 2; ++side) {
+                            const float us[NF] = {side ? uc[0].y : uc[0].x, side ? uc[1].y : uc[1].x,
+                                                  side ? uc[2].y : uc[2].x};
+                            const float u0s[NF] = {side ? u0[0].y : u0[0].x, side ? u0[1].y : u0[1].x,
+                                                   side ? u0[2].y : u0[2].x};
+                            source_terms<NF, float, false>(P, B, us, u0s, x, side ? yc2.y : yc2.x, time, dt, it);
 #pragma unroll
-                        for (int f = 0; f < NF; ++f) ts[f] += it[SINK1 * NF + f] + it[SINK2 * NF + f];
+                            for (int f = 0; f < NF; ++f) {
+                                const float sk = it[SINK1 * NF + f] + it[SINK2 * NF + f];
+                                if (side) tot[f].y += sk;
+                                else tot[f].x += sk;
+                                led1[f] += it[SINK1 * NF + f];
+                                led1[NF + f] += it[SINK2 * NF + f];
+                            }
+                        }
                     }
+                    // fake mass: u0 rate dt unless Sigma < Sigma_0 threshold
                     if (fake_on) {
+                        const bool offa = uc[0].x < u0[0].x * P.fake_thr, offb = uc[0].y < u0[0].y * P.fake_thr;
 #pragma unroll
-                        for (int f = 0; f < NF; ++f) ts[f] += it[FAKE_MASS * NF + f];
-                    }
-#pragma unroll
-                    for (int f = 0; f < NF; ++f) {
-                        if (side) tot[f].y = ts[f];
-                        else tot[f].x = ts[f];
-                    }
-                    // this pair's share of the ledger, per group
-                    int m0 = 0, m1 = 0, m2 = 0;
-#pragma unroll
-                    for (int k2 = 0; k2 < NL; ++k2) {
-                        if (!item_live<NF>(k2)) continue;
-                        if (item_group<NF>(k2) == 0) led0[m0++] += it[k2];
-                        else if (item_group<NF>(k2) == 1) { if (sinks_on) led1[m1] += it[k2]; ++m1; }
-                        else { if (fake_on) led2[m2] += it[k2]; ++m2; }
+                        for (int f = 0; f < NF; ++f) {
+                            const float2 fk = mul2(mul2(u0[f], f2(P.fake_rate)), f2(dt));
+                            const float fa = offa ? 0.0f : fk.x, fb = offb ? 0.0f : fk.y;
+                            tot[f] = add2(tot[f], make_float2(fa, fb));
+                            led2[f] = fa + fb;
+                        }
                     }
                 }
                 // flux divergence and the compensated RK update (scheme.rs:290-305; state.rs:183-199)
@@ -514,7 +549,7 @@ __global__ void __launch_bounds__(96, 4) stage3_kernel(StageArgs a)
                     for (int m = 0; m < 8; ++m) v0[m] = led0[m];
                     const float s0 = warp_sum_items<8>(v0, lane);
                     if (slot0 >= 0) sLed[warp][slot0] += s0;
-                    if (__any_sync(0xffffffffu, sinks_any)) {
+                    if (sinks_any) {
                         float v1[8];
 #pragma unroll
                         for (int m = 0; m < 8; ++m) v1[m] = led1[m];
