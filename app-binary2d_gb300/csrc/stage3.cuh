@@ -302,6 +302,7 @@ __global__ void __launch_bounds__(96, 4) stage3_kernel(StageArgs a)
 
     float2 Pm1[NF], P0[NF];           // primitives of rows rg-1, rg (own pair)
     float2 fxA[NF], fxB[NF];          // x fluxes at faces ru-1/2, ru+1/2
+    float2 xg[NF], xtn = f2(0.0f), xtt = f2(0.0f);   // row rg's x slopes and stresses, for this row's x faces
     constexpr int NLIVE = live_items<NF>();
     static_assert(group_size<NF, 0>() + group_size<NF, 1>() + group_size<NF, 2>() == NLIVE, "ledger groups");
     __shared__ float sLed[4][32];
@@ -313,7 +314,7 @@ __global__ void __launch_bounds__(96, 4) stage3_kernel(StageArgs a)
     const bool fake_on = P.fake_rate != 0.0f;
     float amax = 0.0f;
 #pragma unroll
-    for (int f = 0; f < NF; ++f) { Pm1[f] = P0[f] = fxA[f] = fxB[f] = f2(0.0f); }
+    for (int f = 0; f < NF; ++f) { Pm1[f] = P0[f] = fxA[f] = fxB[f] = xg[f] = f2(0.0f); }
 
     for (int k = 0; k < TH + 5; ++k) {
         const int rn = k - 2;
@@ -385,6 +386,10 @@ __global__ void __launch_bounds__(96, 4) stage3_kernel(StageArgs a)
             sR0[o + 1] = make_float4(P0[0].y, P0[1].y, P0[2].y, gy[0].y);
             sR1[o + 1] = make_float4(gy[1].y, gy[2].y, tyy.y, txy.y);
             sR2[o + 1] = make_float4(gx[0].y, gx[1].y, gx[2].y, txx.y);
+#pragma unroll
+            for (int f = 0; f < NF; ++f) xg[f] = gx[f];
+            xtn = txx;
+            xtt = txy;
         }
         if (rn <= TH + 1) {
 #pragma unroll
@@ -570,21 +575,20 @@ __global__ void __launch_bounds__(96, 4) stage3_kernel(StageArgs a)
                 }
             }
 
-            // x fluxes of faces rq + 1/2 below the pair: own records of rows rq and rq + 1
+            // x fluxes of faces rq + 1/2 below the pair: row rq's records from shared
+            // memory, row rq + 1 = rg's from this iteration's registers (primitives
+            // in Pm1 after the rotation)
             {
-                const int oa = (rq & 1) * (TW + 4) + c0 + 2, ob = ((rq + 1) & 1) * (TW + 4) + c0 + 2;
+                const int oa = (rq & 1) * (TW + 4) + c0 + 2;
                 const float4 a0 = sR0[oa], a1 = sR1[oa], a2 = sR2[oa], e0 = sR0[oa + 1], e1 = sR1[oa + 1], e2 = sR2[oa + 1];
-                const float4 b0 = sR0[ob], b1 = sR1[ob], b2 = sR2[ob], h0 = sR0[ob + 1], h1 = sR1[ob + 1], h2 = sR2[ob + 1];
                 const float2 pcl[3] = {make_float2(a0.x, e0.x), make_float2(a0.y, e0.y), make_float2(a0.z, e0.z)};
                 const float2 gl[3] = {make_float2(a2.x, e2.x), make_float2(a2.y, e2.y), make_float2(a2.z, e2.z)};
-                const float2 pcr[3] = {make_float2(b0.x, h0.x), make_float2(b0.y, h0.y), make_float2(b0.z, h0.z)};
-                const float2 gr[3] = {make_float2(b2.x, h2.x), make_float2(b2.y, h2.y), make_float2(b2.z, h2.z)};
                 const float x = xv_row[min(max(rq + 1, 0), TH)];
                 const float d1x = x - B.p1.x, d2x = x - B.p2.x;
                 const float2 cs2 =
                     iso_face_cs2_2(P, B, d1x * d1x, d2x * d2x, col_part(yc2, B.p1.y), col_part(yc2, B.p2.y));
-                face_flux2<0>(P, B, pcl, gl, make_float2(a2.w, e2.w), make_float2(a1.w, e1.w), pcr, gr,
-                              make_float2(b2.w, h2.w), make_float2(b1.w, h1.w), f2(x), yc2, cs2, fxn);
+                face_flux2<0>(P, B, pcl, gl, make_float2(a2.w, e2.w), make_float2(a1.w, e1.w), Pm1, xg, xtn, xtt,
+                              f2(x), yc2, cs2, fxn);
             }
         } else if (hl == 1 && fy_ok) {
             y_flux();
