@@ -52,7 +52,7 @@ def peaks():
 def ncu_traffic(workload, precision):
     """DRAM bytes (read + write) of one stage-kernel launch from the committed
     ncu summary of this workload, or None."""
-    name = {("disk_2048", "fp32_comp"): "stage2_kernel_fp32comp_disk2048.md"}.get((workload, precision))
+    name = {("disk_2048", "fp32_comp"): "stage3_kernel_fp32comp_disk2048.md"}.get((workload, precision))
     if not name:
         return None
     try:
@@ -352,12 +352,13 @@ def ours(args):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                          "frac": achieved / hbm_peak, "peak_kind": peak_kind,
                          "traffic": ncu_traffic(args.workload, prec),
-                         "traffic_note": ("DRAM bytes of one first-stage launch (72 B/zone algorithmic, "
-                                          "302 MB) from profiles/stage2_kernel_fp32comp_disk2048.md")
+                         "traffic_note": ("mean DRAM bytes of the two RK2 stage launches of one step "
+                                          "(algorithmic mean 352 MB) from profiles/stage3_kernel_fp32comp_disk2048.md")
                                          if ncu_traffic(args.workload, prec) else "no ncu capture of this workload",
                          "algorithmic_bytes_per_launch": bytes_per_launch,
                          "bytes_per_zone_update": bytes_per_zone_update, "stage_ms": stage_ms,
-                         "limiter": "FP32 instruction issue (ncu: 71% issue active, DRAM 14% of peak)"},
+                         "limiter": ("instruction issue and latency at 12 warps/SM (ncu: 49% issue active, "
+                                     "686 warp instructions per zone-stage, DRAM 17-24% of peak)")},
             "fp64": {"value": fp64_value, "ratio": (value / fp64_value) if fp64_value else None},
             "accuracy": accuracy,
             "cpu_baseline": cpu,
