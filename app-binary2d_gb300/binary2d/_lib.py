@@ -50,7 +50,8 @@ class B2DDiskModel(ctypes.Structure):
         ("surface_density", c_double), ("mach_number", c_double), ("cavity_radius", c_double),
         ("cavity_floor", c_double), ("noise", c_double), ("seed", ctypes.c_uint64),
         ("run", c_int32), ("kind", c_int32), ("disk_mass", c_double), ("disk_width", c_double),
-        ("disk_radius", c_double), ("disk_softening", c_double),
+        ("disk_radius", c_double), ("disk_softening", c_double), ("core_radius", c_double),
+        ("edge_width", c_double),
     ]
 
 

@@ -104,8 +104,14 @@ class DiskModel:
     """An initial model of AnyModel (src/app.rs:41-48): `kind` is one of
     infinite_disk (disks.rs:137-157), infinite_alpha_disk (172-193),
     finite_disk (11-115; disk_mass, disk_width, disk_radius,
-    softening_length) or residual_test (208-228).  The synthetic cavity and
-    seeded multiplicative Σ noise are additions (the reference has neither)."""
+    softening_length) or residual_test (208-228).  The synthetic cavity,
+    seeded multiplicative Σ noise and the rotating core are additions (the
+    reference has none of them): inside `core_radius` the gas rotates as a
+    solid body at the core edge's Keplerian rate, v and c_s scaled by
+    (r / core_radius)^(3/2), instead of the model's r^(-1/2), which diverges
+    at the origin; with `edge_width` the velocity is brought to rest at the
+    domain edge, v * (1 - tanh((r - (R - w)) / (0.3 w))) / 2, so that the
+    periodic boundary does not join counter-rotating flows."""
     surface_density: float = 1.0
     mach_number: Optional[float] = None
     cavity_radius: float = 0.0
@@ -117,6 +123,8 @@ class DiskModel:
     disk_width: float = 1.0
     disk_radius: float = 1.0
     softening_length: float = 0.0
+    core_radius: float = 0.0
+    edge_width: float = 0.0
 
 
 def to_c(mesh: Mesh, hydro, physics: Physics) -> B2DConfig:

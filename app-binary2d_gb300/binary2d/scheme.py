@@ -79,6 +79,8 @@ def initial_state(mesh: Mesh, hydro, physics: Physics, model: DiskModel, run: in
     m.disk_width = model.disk_width
     m.disk_radius = model.disk_radius
     m.disk_softening = model.softening_length
+    m.core_radius = model.core_radius
+    m.edge_width = model.edge_width
     nf = num_fields(hydro)
     out = np.empty((mesh.num_blocks, mesh.num_blocks, mesh.block_size, mesh.block_size, nf), dtype=np.float64)
     _check(lib.b2d_initial_state(ctypes.byref(c), ctypes.byref(m), _dp(out)))

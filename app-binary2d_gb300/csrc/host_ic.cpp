@@ -129,6 +129,20 @@ extern "C" b2d_status b2d_initial_state(const b2d_config* c, const b2d_disk_mode
                         double p[4];
                         b2d::model_primitive(c, m, x, y, p);
                         double sd = p[0], vx = p[1], vy = p[2], pg = p[3];
+                        if (r < m->core_radius) {
+                            // solid-body core: v and c_s scaled by (r / r_core)^(3/2)
+                            double s = std::pow(r / m->core_radius, 1.5);
+                            vx = vx * s;
+                            vy = vy * s;
+                            pg = pg * (s * s);
+                        }
+                        if (m->edge_width > 0.0) {
+                            // synthetic: at rest at the domain edge
+                            const double w = m->edge_width;
+                            const double f = 0.5 * (1.0 - std::tanh((r - (c->domain_radius - w)) / (0.3 * w)));
+                            vx = vx * f;
+                            vy = vy * f;
+                        }
                         if (m->cavity_radius > 0.0) {
                             double f = std::fmax(m->cavity_floor, std::exp(-std::pow(m->cavity_radius / r, 12.0)));
                             sd = sd * f;

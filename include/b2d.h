@@ -257,6 +257,9 @@ typedef struct b2d_disk_model {
     double   disk_width;
     double   disk_radius;
     double   disk_softening;
+    double   core_radius;      /* synthetic: solid-body rotation inside this radius (0: none) */
+    double   edge_width;       /* synthetic: velocity tapered to rest over this width inside
+                                  the domain radius (0: none)                 */
 } b2d_disk_model;
 
 b2d_status b2d_initial_state(const b2d_config* cfg, const b2d_disk_model* model,

@@ -1239,6 +1239,20 @@ int oracle_initial_state(const oracle_config* c, const oracle_disk_model* m, dou
                     double r = sqrt(x * x + y * y);
                     double p[4];
                     model_primitive(c, m, x, y, p);
+                    if (r < m->core_radius) {
+                        /* synthetic solid-body core: v and c_s scaled by (r / r_core)^(3/2) */
+                        double s = pow(r / m->core_radius, 1.5);
+                        p[1] = p[1] * s;
+                        p[2] = p[2] * s;
+                        p[3] = p[3] * (s * s);
+                    }
+                    if (m->edge_width > 0.0) {
+                        /* synthetic: at rest at the domain edge */
+                        double w = m->edge_width;
+                        double f = 0.5 * (1.0 - tanh((r - (c->domain_radius - w)) / (0.3 * w)));
+                        p[1] = p[1] * f;
+                        p[2] = p[2] * f;
+                    }
                     if (m->cavity_radius > 0.0) {
                         double f = fmax(m->cavity_floor, exp(-pow(m->cavity_radius / r, 12.0)));
                         p[0] = p[0] * f;

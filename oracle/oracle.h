@@ -91,6 +91,8 @@ typedef struct oracle_disk_model {
     double   disk_width;
     double   disk_radius;
     double   disk_softening;
+    double   core_radius;
+    double   edge_width;
 } oracle_disk_model;
 
 /* m, x, y, vx, vy of each body */

@@ -68,12 +68,14 @@ def test_all_initial_models_match_oracle_bitwise(kind):
     for hydro in (b2.Isothermal(mach_number=10.0), b2.Euler(gamma_law_index=1.66666666666666)):
         physics = b2.presets.iso_physics()
         model = b2.DiskModel(surface_density=1.0, mach_number=8.0, kind=kind, disk_mass=1e-3, disk_width=3.0,
-                             disk_radius=3.0, softening_length=0.05, noise=1e-3, seed=7, cavity_radius=1.0)
+                             disk_radius=3.0, softening_length=0.05, noise=1e-3, seed=7, cavity_radius=1.0,
+                             core_radius=0.7, edge_width=1.5)
         cons = b2.initial_state(mesh, hydro, physics, model)
         cfg = b2.to_c(mesh, hydro, physics)
         m = _lib.B2DDiskModel(surface_density=1.0, mach_number=8.0, cavity_radius=1.0, cavity_floor=1e-4,
                               noise=1e-3, seed=7, run=0, kind=b2.config.MODEL_KINDS[kind], disk_mass=1e-3,
-                              disk_width=3.0, disk_radius=3.0, disk_softening=0.05)
+                              disk_width=3.0, disk_radius=3.0, disk_softening=0.05, core_radius=0.7,
+                              edge_width=1.5)
         ref = binding.initial_state(cfg, m, cons.shape)
         assert np.array_equal(cons, ref)
         assert np.all(np.isfinite(cons)) and np.all(cons[..., 0] > 0)
