@@ -159,45 +159,69 @@ __global__ void max_speed_kernel(const RunDev* runs, int run, int slot)
     if (threadIdx.x == 0 && red[0] > 0.0) atomicMax(rd.amax, (unsigned long long)__double_as_longlong(red[0]));
 }
 
-// Block layout [nb][nb][bs][bs][nf] (host) <-> field planes (device).
-__device__ __forceinline__ size_t block_index(int gi, int gj, int bs, int nb, int nf)
+// Block layout [nb][nb][bs][bs][nf] (host) <-> field planes (device).  One
+// thread per element of the block layout, so the host-side side of the copy
+// (which may be a page-locked host buffer read or written in place over the
+// CPU-GPU link) is one contiguous, fully coalesced sweep.
+__device__ __forceinline__ size_t plane_index(size_t zb, int N, int bs, int nb)
 {
-    int bi = gi / bs, bj = gj / bs, li = gi % bs, lj = gj % bs;
-    return ((((size_t)bi * nb + bj) * bs + li) * bs + lj) * nf;
+    const size_t lj = zb % bs, li = (zb / bs) % bs, blk = zb / ((size_t)bs * bs);
+    const size_t bj = blk % nb, bi = blk / nb;
+    return (bi * bs + li) * (size_t)N + bj * bs + lj;
+}
+
+// Two elements per thread and 16-byte accesses on the host side; both
+// buffers must be 16-byte aligned (the callers check), an odd last element
+// is done by thread 0.
+__device__ __forceinline__ void scatter_one(double v, size_t e, void* dst, size_t nn, int N, int bs, int nb, int nf,
+                                            int store)
+{
+    const size_t zb = e / nf;
+    const int f = (int)(e - zb * nf);
+    const size_t z = plane_index(zb, N, bs, nb);
+    if (store == 0) {
+        ((double*)dst)[f * nn + z] = v;
+    } else {
+        const float hi = (float)v;
+        const float lo = (float)(v - (double)hi);
+        ((float*)dst)[(2 * f) * nn + z] = hi;
+        ((float*)dst)[(2 * f + 1) * nn + z] = lo;
+    }
+}
+
+__device__ __forceinline__ double gather_one(const void* src, size_t e, size_t nn, int N, int bs, int nb, int nf,
+                                             int store)
+{
+    const size_t zb = e / nf;
+    const int f = (int)(e - zb * nf);
+    const size_t z = plane_index(zb, N, bs, nb);
+    if (store == 0) return ((const double*)src)[f * nn + z];
+    return (double)((const float*)src)[(2 * f) * nn + z] + (double)((const float*)src)[(2 * f + 1) * nn + z];
 }
 
 __global__ void scatter_kernel(const double* src, void* dst, int N, int bs, int nb, int nf, int store)
 {
-    const size_t nn = (size_t)N * N;
-    for (size_t z = blockIdx.x * (size_t)blockDim.x + threadIdx.x; z < nn; z += (size_t)gridDim.x * blockDim.x) {
-        int gi = (int)(z / N), gj = (int)(z % N);
-        size_t b = block_index(gi, gj, bs, nb, nf);
-        for (int f = 0; f < nf; ++f) {
-            double v = src[b + f];
-            if (store == 0) ((double*)dst)[f * nn + z] = v;
-            else {
-                float hi = (float)v;
-                float lo = (float)(v - (double)hi);
-                ((float*)dst)[(2 * f) * nn + z] = hi;
-                ((float*)dst)[(2 * f + 1) * nn + z] = lo;
-            }
-        }
+    const size_t nn = (size_t)N * N, np = nn * nf / 2;
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < np; k += (size_t)gridDim.x * blockDim.x) {
+        const double2 v = ((const double2*)src)[k];
+        scatter_one(v.x, 2 * k, dst, nn, N, bs, nb, nf, store);
+        scatter_one(v.y, 2 * k + 1, dst, nn, N, bs, nb, nf, store);
     }
+    if (((nn * nf) & 1) && blockIdx.x == 0 && threadIdx.x == 0)
+        scatter_one(src[nn * nf - 1], nn * nf - 1, dst, nn, N, bs, nb, nf, store);
 }
 
 __global__ void gather_kernel(const void* src, double* dst, int N, int bs, int nb, int nf, int store)
 {
-    const size_t nn = (size_t)N * N;
-    for (size_t z = blockIdx.x * (size_t)blockDim.x + threadIdx.x; z < nn; z += (size_t)gridDim.x * blockDim.x) {
-        int gi = (int)(z / N), gj = (int)(z % N);
-        size_t b = block_index(gi, gj, bs, nb, nf);
-        for (int f = 0; f < nf; ++f) {
-            double v;
-            if (store == 0) v = ((const double*)src)[f * nn + z];
-            else v = (double)((const float*)src)[(2 * f) * nn + z] + (double)((const float*)src)[(2 * f + 1) * nn + z];
-            dst[b + f] = v;
-        }
+    const size_t nn = (size_t)N * N, np = nn * nf / 2;
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < np; k += (size_t)gridDim.x * blockDim.x) {
+        double2 v;
+        v.x = gather_one(src, 2 * k, nn, N, bs, nb, nf, store);
+        v.y = gather_one(src, 2 * k + 1, nn, N, bs, nb, nf, store);
+        ((double2*)dst)[k] = v;
     }
+    if (((nn * nf) & 1) && blockIdx.x == 0 && threadIdx.x == 0)
+        dst[nn * nf - 1] = gather_one(src, nn * nf - 1, nn, N, bs, nb, nf, store);
 }
 
 // ---------------------------------------------------------------------------
@@ -650,13 +674,33 @@ extern "C" b2d_status b2d_upload_state(b2d_ctx* ctx, int32_t run, const double* 
     return B2D_OK;
 }
 
+// Device address of a page-locked (cudaHostRegister / cudaMallocHost) host
+// buffer that is 16-byte aligned, or nullptr.  The layout kernels read and
+// write such buffers in place over the CPU-GPU link, so the copy and the
+// layout change are one pass; other buffers go through the device staging
+// buffer.
+static void* mapped_host(const void* p)
+{
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (at.type != cudaMemoryTypeHost || !at.devicePointer || ((uintptr_t)at.devicePointer & 15u)) return nullptr;
+    return at.devicePointer;
+}
+
 extern "C" b2d_status b2d_upload_conserved(b2d_ctx* ctx, int32_t run, const double* cons)
 {
     if (!ctx || run < 0 || run >= ctx->nruns || !cons) return fail(B2D_ERR_INVALID, "bad arguments");
     RunHost& r = ctx->runs[run];
     size_t n = (size_t)r.N * r.N * ctx->nf;
-    CUDA_TRY(cudaMemcpyAsync(ctx->d_staging, cons, n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-    scatter_kernel<<<4 * 152, 256, 0, ctx->stream>>>(ctx->d_staging, r.slot[ctx->cur], r.N, r.bs, r.nb, ctx->nf, store_of(ctx));
+    const double* src = (const double*)mapped_host(cons);
+    if (!src) {
+        CUDA_TRY(cudaMemcpyAsync(ctx->d_staging, cons, n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+        src = ctx->d_staging;
+    }
+    scatter_kernel<<<16 * 152, 256, 0, ctx->stream>>>(src, r.slot[ctx->cur], r.N, r.bs, r.nb, ctx->nf, store_of(ctx));
     ctx->launches++;
     CUDA_TRY(cudaGetLastError());
     b2d_status s = launch_max_speed(ctx, run, ctx->cur);
@@ -672,10 +716,12 @@ extern "C" b2d_status b2d_download_state(b2d_ctx* ctx, int32_t run, double* cons
     RunHost& r = ctx->runs[run];
     size_t n = (size_t)r.N * r.N * ctx->nf;
     if (cons) {
-        gather_kernel<<<4 * 152, 256, 0, ctx->stream>>>(r.slot[ctx->cur], ctx->d_staging, r.N, r.bs, r.nb, ctx->nf, store_of(ctx));
+        double* dst = (double*)mapped_host(cons);
+        gather_kernel<<<16 * 152, 256, 0, ctx->stream>>>(r.slot[ctx->cur], dst ? dst : ctx->d_staging, r.N, r.bs, r.nb,
+                                                         ctx->nf, store_of(ctx));
         ctx->launches++;
         CUDA_TRY(cudaGetLastError());
-        CUDA_TRY(cudaMemcpyAsync(cons, ctx->d_staging, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        if (!dst) CUDA_TRY(cudaMemcpyAsync(cons, ctx->d_staging, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     }
     double t = 0;
     long long it = 0;
