@@ -86,6 +86,9 @@ _SIGNATURES = [
     ("b2d_unpin_host", c_int32, [ctypes.c_void_p]),
     ("b2d_set_device", c_int32, [c_int32]),
     ("b2d_download_elements", c_int32, [ctypes.c_void_p, c_int32, c_dp]),
+    ("b2d_upload_conserved_async", c_int32, [ctypes.c_void_p, c_int32, c_dp]),
+    ("b2d_download_async", c_int32, [ctypes.c_void_p, c_int32, c_dp]),
+    ("b2d_transfers_wait", c_int32, [ctypes.c_void_p, c_int32]),
     ("b2d_upload_elements", c_int32, [ctypes.c_void_p, c_int32, c_dp]),
     ("b2d_set_tracers", c_int32, [ctypes.c_void_p, c_int32, c_int64, c_dp]),
     ("b2d_get_tracers", c_int32, [ctypes.c_void_p, c_int32, c_dp]),

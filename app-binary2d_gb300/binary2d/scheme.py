@@ -132,6 +132,22 @@ class Runtime:
         cons = np.ascontiguousarray(cons, dtype=np.float64)
         _check(self.lib.b2d_upload_conserved(self.ctx, run, _dp(cons)))
 
+    def upload_conserved_async(self, run: int, cons: np.ndarray):
+        """Queue an upload of `cons` (contiguous float64, ideally pinned); it
+        must stay unchanged until a later download has landed."""
+        assert cons.flags.c_contiguous and cons.dtype == np.float64
+        _check(self.lib.b2d_upload_conserved_async(self.ctx, run, _dp(cons)))
+
+    def download_async(self, run: int, out: np.ndarray):
+        """Queue a download of the state (as queued so far) into `out`."""
+        assert out.flags.c_contiguous and out.dtype == np.float64
+        _check(self.lib.b2d_download_async(self.ctx, run, _dp(out)))
+
+    def transfers_wait(self, pending: int = 0):
+        """Block until every transfer (pending=0) or every download but the
+        newest (pending=1) has landed."""
+        _check(self.lib.b2d_transfers_wait(self.ctx, int(pending)))
+
     def download(self, run: int = 0, out: Optional[np.ndarray] = None) -> Tuple[np.ndarray, float, int]:
         m = self.runs[run].mesh
         if out is None:

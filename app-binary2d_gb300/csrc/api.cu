@@ -280,6 +280,13 @@ struct b2d_ctx {
     std::vector<std::pair<int, std::vector<StagePlan>>> window;  // advances since the last check
     double* d_staging = nullptr;
     size_t staging_bytes = 0;
+    // pipelined host transfers (b2d_upload_conserved_async / b2d_download_async):
+    // copy streams, double-buffered device staging and their events
+    cudaStream_t up_stream = nullptr, down_stream = nullptr;
+    double* d_in[2] = {};
+    double* d_out[2] = {};
+    cudaEvent_t in_copied[2] = {}, in_used[2] = {}, out_ready[2] = {}, out_copied[2] = {};
+    long long n_up = 0, n_down = 0;
     int max_stages = 0;
     cudaStream_t stream = nullptr;
     bool use_graphs = true;
@@ -418,6 +425,14 @@ static void free_ctx(b2d_ctx* ctx)
     cudaFree(ctx->d_amax); cudaFree(ctx->d_err_key); cudaFree(ctx->d_adv_count); cudaFree(ctx->d_timeout); cudaFree(ctx->d_staging);
     for (cudaEvent_t e : ctx->ev) cudaEventDestroy(e);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    if (ctx->up_stream) cudaStreamDestroy(ctx->up_stream);
+    if (ctx->down_stream) cudaStreamDestroy(ctx->down_stream);
+    for (int b = 0; b < 2; ++b) {
+        cudaFree(ctx->d_in[b]);
+        cudaFree(ctx->d_out[b]);
+        for (cudaEvent_t e : {ctx->in_copied[b], ctx->in_used[b], ctx->out_ready[b], ctx->out_copied[b]})
+            if (e) cudaEventDestroy(e);
+    }
     delete ctx;
 }
 
@@ -706,6 +721,83 @@ extern "C" b2d_status b2d_upload_conserved(b2d_ctx* ctx, int32_t run, const doub
     b2d_status s = launch_max_speed(ctx, run, ctx->cur);
     if (s != B2D_OK) return s;
     CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return B2D_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Pipelined host transfers.  Two copy streams move page-locked host buffers
+// through double-buffered device staging while the context stream computes;
+// the context stream only runs the layout kernels, so a step of a pipelined
+// loop costs scatter + advance + gather on the device and the copies overlap
+// the neighbouring steps' advances.
+
+static b2d_status ensure_pipeline(b2d_ctx* ctx)
+{
+    if (ctx->up_stream) return B2D_OK;
+    CUDA_TRY(cudaStreamCreateWithFlags(&ctx->up_stream, cudaStreamNonBlocking));
+    CUDA_TRY(cudaStreamCreateWithFlags(&ctx->down_stream, cudaStreamNonBlocking));
+    for (int b = 0; b < 2; ++b) {
+        CUDA_TRY(cudaMalloc(&ctx->d_in[b], ctx->staging_bytes));
+        CUDA_TRY(cudaMalloc(&ctx->d_out[b], ctx->staging_bytes));
+        for (cudaEvent_t* e : {&ctx->in_copied[b], &ctx->in_used[b], &ctx->out_ready[b], &ctx->out_copied[b]})
+            CUDA_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    }
+    return B2D_OK;
+}
+
+extern "C" b2d_status b2d_upload_conserved_async(b2d_ctx* ctx, int32_t run, const double* cons)
+{
+    if (!ctx || run < 0 || run >= ctx->nruns || !cons) return fail(B2D_ERR_INVALID, "bad arguments");
+    b2d_status st = ensure_pipeline(ctx);
+    if (st != B2D_OK) return st;
+    RunHost& r = ctx->runs[run];
+    const size_t n = (size_t)r.N * r.N * ctx->nf;
+    const int b = (int)(ctx->n_up++ & 1);
+    // the staging buffer is free once the scatter that last read it has run
+    CUDA_TRY(cudaStreamWaitEvent(ctx->up_stream, ctx->in_used[b], 0));
+    CUDA_TRY(cudaMemcpyAsync(ctx->d_in[b], cons, n * sizeof(double), cudaMemcpyHostToDevice, ctx->up_stream));
+    CUDA_TRY(cudaEventRecord(ctx->in_copied[b], ctx->up_stream));
+    CUDA_TRY(cudaStreamWaitEvent(ctx->stream, ctx->in_copied[b], 0));
+    scatter_kernel<<<16 * 152, 256, 0, ctx->stream>>>(ctx->d_in[b], r.slot[ctx->cur], r.N, r.bs, r.nb, ctx->nf,
+                                                       store_of(ctx));
+    ctx->launches++;
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaEventRecord(ctx->in_used[b], ctx->stream));
+    return launch_max_speed(ctx, run, ctx->cur);
+}
+
+extern "C" b2d_status b2d_download_async(b2d_ctx* ctx, int32_t run, double* cons)
+{
+    if (!ctx || run < 0 || run >= ctx->nruns || !cons) return fail(B2D_ERR_INVALID, "bad arguments");
+    b2d_status st = ensure_pipeline(ctx);
+    if (st != B2D_OK) return st;
+    RunHost& r = ctx->runs[run];
+    const size_t n = (size_t)r.N * r.N * ctx->nf;
+    const int b = (int)(ctx->n_down++ & 1);
+    // the staging buffer is free once the copy that last read it has finished
+    CUDA_TRY(cudaStreamWaitEvent(ctx->stream, ctx->out_copied[b], 0));
+    gather_kernel<<<16 * 152, 256, 0, ctx->stream>>>(r.slot[ctx->cur], ctx->d_out[b], r.N, r.bs, r.nb, ctx->nf,
+                                                      store_of(ctx));
+    ctx->launches++;
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaEventRecord(ctx->out_ready[b], ctx->stream));
+    CUDA_TRY(cudaStreamWaitEvent(ctx->down_stream, ctx->out_ready[b], 0));
+    CUDA_TRY(cudaMemcpyAsync(cons, ctx->d_out[b], n * sizeof(double), cudaMemcpyDeviceToHost, ctx->down_stream));
+    CUDA_TRY(cudaEventRecord(ctx->out_copied[b], ctx->down_stream));
+    return B2D_OK;
+}
+
+extern "C" b2d_status b2d_transfers_wait(b2d_ctx* ctx, int32_t pending)
+{
+    if (!ctx || pending < 0 || pending > 1) return fail(B2D_ERR_INVALID, "bad arguments");
+    if (!ctx->up_stream) return B2D_OK;
+    if (pending == 0) {
+        CUDA_TRY(cudaStreamSynchronize(ctx->up_stream));
+        CUDA_TRY(cudaStreamSynchronize(ctx->down_stream));
+        return B2D_OK;
+    }
+    // every download but the newest has landed (downloads complete in order)
+    if (ctx->n_down >= 2) CUDA_TRY(cudaEventSynchronize(ctx->out_copied[(ctx->n_down - 2) & 1]));
     return B2D_OK;
 }
 

@@ -191,6 +191,21 @@ b2d_status b2d_download_ledger(b2d_ctx* ctx, int32_t run, double* ledger);
  * [num_blocks][num_blocks][7][4] of (a, M, q, e) per ledger item.  Uploading
  * a state resets it to zero; these calls move it to and from the host. */
 b2d_status b2d_download_elements(b2d_ctx* ctx, int32_t run, double* elements);
+
+/* Pipelined host transfers (no reference counterpart: the reference keeps its
+ * state in host memory).  Both calls return at once; the bytes move on two
+ * copy streams through double-buffered device staging while the context's
+ * stream computes, so in a loop of upload / advance_async / download the
+ * copies of one step overlap the neighbouring steps' advances.  Buffers
+ * should be page-locked (b2d_pin_host) for the copies to be asynchronous.
+ *   b2d_upload_conserved_async — like b2d_upload_conserved, queued: `cons`
+ *     must stay unchanged until a download queued after it has landed;
+ *   b2d_download_async — the state as queued at this point, into `cons`;
+ *   b2d_transfers_wait — pending = 0: every queued transfer has landed;
+ *   pending = 1: every download but the newest has landed. */
+b2d_status b2d_upload_conserved_async(b2d_ctx* ctx, int32_t run, const double* cons);
+b2d_status b2d_download_async(b2d_ctx* ctx, int32_t run, double* cons);
+b2d_status b2d_transfers_wait(b2d_ctx* ctx, int32_t pending);
 b2d_status b2d_upload_elements(b2d_ctx* ctx, int32_t run, const double* elements);
 
 /* ------------------------------------------------------------------------ */

@@ -165,3 +165,39 @@ def test_layout_roundtrip_odd_element_count(precision):
     if precision == "fp64":
         assert np.array_equal(out, cons)
     assert np.array_equal(dst, out)
+
+
+def test_pipelined_transfers_match_synchronous():
+    """upload_async / advance_async / download_async in a loop, two steps in
+    flight: each step's result is bitwise the synchronous loop's."""
+    mesh, hydro, physics, model = b2.presets.iso_disk(4, 64, seed=19)
+    cons, _ = make_case(mesh, hydro, physics, model)
+    inputs = [cons * (1.0 + 1e-3 * k) for k in range(4)]
+    with b2.Runtime([b2.Run(mesh, hydro, physics)], precision="fp32_comp") as rt:
+        rt.upload(0, cons)
+        want = []
+        for x in inputs:
+            rt.upload_conserved(0, x)
+            rt.advance(2)
+            want.append(rt.download(0)[0].copy())
+    src = [np.ascontiguousarray(x) for x in inputs]
+    dst = [np.zeros_like(x) for x in inputs]
+    for a in src + dst:
+        b2.pin(a)
+    try:
+        with b2.Runtime([b2.Run(mesh, hydro, physics)], precision="fp32_comp") as rt:
+            rt.upload(0, cons)
+            for k in range(len(src)):
+                rt.upload_conserved_async(0, src[k])
+                rt.advance_async(2)
+                rt.download_async(0, dst[k])
+                rt.transfers_wait(1)
+                if k >= 1:
+                    assert np.array_equal(dst[k - 1], want[k - 1])
+            rt.transfers_wait(0)
+            rt.synchronize()
+    finally:
+        for a in src + dst:
+            b2.unpin(a)
+    for k in range(len(src)):
+        assert np.array_equal(dst[k], want[k])
