@@ -131,23 +131,23 @@ __global__ void prologue_kernel(const RunDev* runs, int fold, int rk, int start,
     for (int s = threadIdx.x; s < fold * stages; s += blockDim.x) kepler_orbit(rd, rd.stage_time[s], rd.orbit + 10 * s);
 }
 
-// State::max_signal_speed (state.rs:121-133) of one run's slot.
-template <int NF, int STORE>
+// State::max_signal_speed (state.rs:121-133) of one run's slot, in the
+// precision the stage kernels use for it at the end of an advance: FP64 for
+// the FP64 path, FP32 of the stored (high) words for the FP32 paths (FP64
+// divisions and roots on a whole mesh are slow on this GPU).
+template <int NF, int STORE, class R>
 __global__ void max_speed_kernel(const RunDev* runs, int run, int slot)
 {
     const RunDev& rd = runs[run];
     const size_t nn = (size_t)rd.N * rd.N;
-    double a = 0.0;
+    R a = R(0);
     for (size_t z = blockIdx.x * (size_t)blockDim.x + threadIdx.x; z < nn; z += (size_t)gridDim.x * blockDim.x) {
-        double u[NF];
+        R u[NF];
         for (int f = 0; f < NF; ++f) {
-            if (STORE == 0) u[f] = ((const double*)rd.slot[slot])[f * nn + z];
-            else {
-                const float* p = (const float*)rd.slot[slot];
-                u[f] = (double)p[(2 * f) * nn + z] + (double)p[(2 * f + 1) * nn + z];
-            }
+            if (STORE == 0) u[f] = (R)((const double*)rd.slot[slot])[f * nn + z];
+            else u[f] = (R)((const float*)rd.slot[slot])[(2 * f) * nn + z];
         }
-        a = fmax(max_signal_speed<NF, double>(rd.p, u), a);
+        a = rmax(max_signal_speed<NF, R>(params_of<R>(rd), u), a);
     }
     __shared__ double red[256];
     red[threadIdx.x] = a;
@@ -159,70 +159,60 @@ __global__ void max_speed_kernel(const RunDev* runs, int run, int slot)
     if (threadIdx.x == 0 && red[0] > 0.0) atomicMax(rd.amax, (unsigned long long)__double_as_longlong(red[0]));
 }
 
-// Block layout [nb][nb][bs][bs][nf] (host) <-> field planes (device).  One
-// thread per element of the block layout, so the host-side side of the copy
-// (which may be a page-locked host buffer read or written in place over the
-// CPU-GPU link) is one contiguous, fully coalesced sweep.
-__device__ __forceinline__ size_t plane_index(size_t zb, int N, int bs, int nb)
+// Block layout [nb][nb][bs][bs][nf] (host) <-> field planes (device).  A CTA
+// row handles one row of one mesh block (grid: nb^2 x bs), its threads the
+// row's bs * nf consecutive host-side elements, so the host side (which may
+// be a page-locked host buffer read or written in place over the CPU-GPU
+// link) is a contiguous, coalesced sweep and the index arithmetic is one
+// division by nf per element.
+__device__ __forceinline__ void row_origin(int N, int bs, int nb, int nf, size_t& e0, size_t& z0)
 {
-    const size_t lj = zb % bs, li = (zb / bs) % bs, blk = zb / ((size_t)bs * bs);
-    const size_t bj = blk % nb, bi = blk / nb;
-    return (bi * bs + li) * (size_t)N + bj * bs + lj;
+    const int blk = blockIdx.x, li = blockIdx.y;
+    const int bi = blk / nb, bj = blk - bi * nb;
+    e0 = ((size_t)blk * bs + li) * (size_t)bs * nf;
+    z0 = (size_t)(bi * bs + li) * N + (size_t)bj * bs;
 }
 
-// Two elements per thread and 16-byte accesses on the host side; both
-// buffers must be 16-byte aligned (the callers check), an odd last element
-// is done by thread 0.
-__device__ __forceinline__ void scatter_one(double v, size_t e, void* dst, size_t nn, int N, int bs, int nb, int nf,
-                                            int store)
-{
-    const size_t zb = e / nf;
-    const int f = (int)(e - zb * nf);
-    const size_t z = plane_index(zb, N, bs, nb);
-    if (store == 0) {
-        ((double*)dst)[f * nn + z] = v;
-    } else {
-        const float hi = (float)v;
-        const float lo = (float)(v - (double)hi);
-        ((float*)dst)[(2 * f) * nn + z] = hi;
-        ((float*)dst)[(2 * f + 1) * nn + z] = lo;
-    }
-}
-
-__device__ __forceinline__ double gather_one(const void* src, size_t e, size_t nn, int N, int bs, int nb, int nf,
-                                             int store)
-{
-    const size_t zb = e / nf;
-    const int f = (int)(e - zb * nf);
-    const size_t z = plane_index(zb, N, bs, nb);
-    if (store == 0) return ((const double*)src)[f * nn + z];
-    return (double)((const float*)src)[(2 * f) * nn + z] + (double)((const float*)src)[(2 * f + 1) * nn + z];
-}
+__device__ __forceinline__ int zone_of(int t, int nf) { return nf == 3 ? t / 3 : t >> 2; }
 
 __global__ void scatter_kernel(const double* src, void* dst, int N, int bs, int nb, int nf, int store)
 {
-    const size_t nn = (size_t)N * N, np = nn * nf / 2;
-    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < np; k += (size_t)gridDim.x * blockDim.x) {
-        const double2 v = ((const double2*)src)[k];
-        scatter_one(v.x, 2 * k, dst, nn, N, bs, nb, nf, store);
-        scatter_one(v.y, 2 * k + 1, dst, nn, N, bs, nb, nf, store);
+    const size_t nn = (size_t)N * N;
+    size_t e0, z0;
+    row_origin(N, bs, nb, nf, e0, z0);
+    for (int t = threadIdx.x; t < bs * nf; t += blockDim.x) {
+        const int lj = zone_of(t, nf), f = t - lj * nf;
+        const double v = src[e0 + t];
+        const size_t z = z0 + lj;
+        if (store == 0) {
+            ((double*)dst)[f * nn + z] = v;
+        } else {
+            const float hi = (float)v;
+            const float lo = (float)(v - (double)hi);
+            ((float*)dst)[(2 * f) * nn + z] = hi;
+            ((float*)dst)[(2 * f + 1) * nn + z] = lo;
+        }
     }
-    if (((nn * nf) & 1) && blockIdx.x == 0 && threadIdx.x == 0)
-        scatter_one(src[nn * nf - 1], nn * nf - 1, dst, nn, N, bs, nb, nf, store);
 }
 
 __global__ void gather_kernel(const void* src, double* dst, int N, int bs, int nb, int nf, int store)
 {
-    const size_t nn = (size_t)N * N, np = nn * nf / 2;
-    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < np; k += (size_t)gridDim.x * blockDim.x) {
-        double2 v;
-        v.x = gather_one(src, 2 * k, nn, N, bs, nb, nf, store);
-        v.y = gather_one(src, 2 * k + 1, nn, N, bs, nb, nf, store);
-        ((double2*)dst)[k] = v;
+    const size_t nn = (size_t)N * N;
+    size_t e0, z0;
+    row_origin(N, bs, nb, nf, e0, z0);
+    for (int t = threadIdx.x; t < bs * nf; t += blockDim.x) {
+        const int lj = zone_of(t, nf), f = t - lj * nf;
+        const size_t z = z0 + lj;
+        double v;
+        if (store == 0) v = ((const double*)src)[f * nn + z];
+        else v = (double)((const float*)src)[(2 * f) * nn + z] + (double)((const float*)src)[(2 * f + 1) * nn + z];
+        dst[e0 + t] = v;
     }
-    if (((nn * nf) & 1) && blockIdx.x == 0 && threadIdx.x == 0)
-        dst[nn * nf - 1] = gather_one(src, nn * nf - 1, nn, N, bs, nb, nf, store);
 }
+
+// Launch shape of the layout kernels for one run.
+static dim3 layout_grid(int nb, int bs) { return dim3((unsigned)(nb * nb), (unsigned)bs); }
+static int layout_threads(int bs, int nf) { return std::min(256, ((bs * nf + 31) / 32) * 32); }
 
 // ---------------------------------------------------------------------------
 // Host-side context.
@@ -645,12 +635,15 @@ static b2d_status launch_max_speed(b2d_ctx* ctx, int run, int slot)
 {
     CUDA_TRY(cudaMemsetAsync(ctx->d_amax + run, 0, sizeof(unsigned long long), ctx->stream));
     int grid = 4 * 152;
+    const bool f64 = ctx->precision == B2D_PREC_FP64;
     if (ctx->nf == 3) {
-        if (store_of(ctx) == 0) max_speed_kernel<3, 0><<<grid, 256, 0, ctx->stream>>>(ctx->rdev, run, slot);
-        else max_speed_kernel<3, 1><<<grid, 256, 0, ctx->stream>>>(ctx->rdev, run, slot);
+        if (f64) max_speed_kernel<3, 0, double><<<grid, 256, 0, ctx->stream>>>(ctx->rdev, run, slot);
+        else if (store_of(ctx) == 0) max_speed_kernel<3, 0, float><<<grid, 256, 0, ctx->stream>>>(ctx->rdev, run, slot);
+        else max_speed_kernel<3, 1, float><<<grid, 256, 0, ctx->stream>>>(ctx->rdev, run, slot);
     } else {
-        if (store_of(ctx) == 0) max_speed_kernel<4, 0><<<grid, 256, 0, ctx->stream>>>(ctx->rdev, run, slot);
-        else max_speed_kernel<4, 1><<<grid, 256, 0, ctx->stream>>>(ctx->rdev, run, slot);
+        if (f64) max_speed_kernel<4, 0, double><<<grid, 256, 0, ctx->stream>>>(ctx->rdev, run, slot);
+        else if (store_of(ctx) == 0) max_speed_kernel<4, 0, float><<<grid, 256, 0, ctx->stream>>>(ctx->rdev, run, slot);
+        else max_speed_kernel<4, 1, float><<<grid, 256, 0, ctx->stream>>>(ctx->rdev, run, slot);
     }
     ctx->launches++;
     CUDA_TRY(cudaGetLastError());
@@ -667,12 +660,12 @@ extern "C" b2d_status b2d_upload_state(b2d_ctx* ctx, int32_t run, const double* 
     int store = store_of(ctx);
     int grid = 4 * 152;
     CUDA_TRY(cudaMemcpyAsync(ctx->d_staging, cons, n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-    scatter_kernel<<<grid, 256, 0, ctx->stream>>>(ctx->d_staging, r.slot[ctx->cur], r.N, r.bs, r.nb, ctx->nf, store);
+    scatter_kernel<<<layout_grid(r.nb, r.bs), layout_threads(r.bs, ctx->nf), 0, ctx->stream>>>(ctx->d_staging, r.slot[ctx->cur], r.N, r.bs, r.nb, ctx->nf, store);
     ctx->launches++;
     CUDA_TRY(cudaGetLastError());
     if (background) {
         CUDA_TRY(cudaMemcpyAsync(ctx->d_staging, background, n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-        scatter_kernel<<<grid, 256, 0, ctx->stream>>>(ctx->d_staging, r.bg, r.N, r.bs, r.nb, ctx->nf, store);
+        scatter_kernel<<<layout_grid(r.nb, r.bs), layout_threads(r.bs, ctx->nf), 0, ctx->stream>>>(ctx->d_staging, r.bg, r.N, r.bs, r.nb, ctx->nf, store);
         ctx->launches++;
         CUDA_TRY(cudaGetLastError());
     }
@@ -715,7 +708,7 @@ extern "C" b2d_status b2d_upload_conserved(b2d_ctx* ctx, int32_t run, const doub
         CUDA_TRY(cudaMemcpyAsync(ctx->d_staging, cons, n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
         src = ctx->d_staging;
     }
-    scatter_kernel<<<16 * 152, 256, 0, ctx->stream>>>(src, r.slot[ctx->cur], r.N, r.bs, r.nb, ctx->nf, store_of(ctx));
+    scatter_kernel<<<layout_grid(r.nb, r.bs), layout_threads(r.bs, ctx->nf), 0, ctx->stream>>>(src, r.slot[ctx->cur], r.N, r.bs, r.nb, ctx->nf, store_of(ctx));
     ctx->launches++;
     CUDA_TRY(cudaGetLastError());
     b2d_status s = launch_max_speed(ctx, run, ctx->cur);
@@ -758,7 +751,7 @@ extern "C" b2d_status b2d_upload_conserved_async(b2d_ctx* ctx, int32_t run, cons
     CUDA_TRY(cudaMemcpyAsync(ctx->d_in[b], cons, n * sizeof(double), cudaMemcpyHostToDevice, ctx->up_stream));
     CUDA_TRY(cudaEventRecord(ctx->in_copied[b], ctx->up_stream));
     CUDA_TRY(cudaStreamWaitEvent(ctx->stream, ctx->in_copied[b], 0));
-    scatter_kernel<<<16 * 152, 256, 0, ctx->stream>>>(ctx->d_in[b], r.slot[ctx->cur], r.N, r.bs, r.nb, ctx->nf,
+    scatter_kernel<<<layout_grid(r.nb, r.bs), layout_threads(r.bs, ctx->nf), 0, ctx->stream>>>(ctx->d_in[b], r.slot[ctx->cur], r.N, r.bs, r.nb, ctx->nf,
                                                        store_of(ctx));
     ctx->launches++;
     CUDA_TRY(cudaGetLastError());
@@ -776,7 +769,7 @@ extern "C" b2d_status b2d_download_async(b2d_ctx* ctx, int32_t run, double* cons
     const int b = (int)(ctx->n_down++ & 1);
     // the staging buffer is free once the copy that last read it has finished
     CUDA_TRY(cudaStreamWaitEvent(ctx->stream, ctx->out_copied[b], 0));
-    gather_kernel<<<16 * 152, 256, 0, ctx->stream>>>(r.slot[ctx->cur], ctx->d_out[b], r.N, r.bs, r.nb, ctx->nf,
+    gather_kernel<<<layout_grid(r.nb, r.bs), layout_threads(r.bs, ctx->nf), 0, ctx->stream>>>(r.slot[ctx->cur], ctx->d_out[b], r.N, r.bs, r.nb, ctx->nf,
                                                       store_of(ctx));
     ctx->launches++;
     CUDA_TRY(cudaGetLastError());
@@ -809,7 +802,7 @@ extern "C" b2d_status b2d_download_state(b2d_ctx* ctx, int32_t run, double* cons
     size_t n = (size_t)r.N * r.N * ctx->nf;
     if (cons) {
         double* dst = (double*)mapped_host(cons);
-        gather_kernel<<<16 * 152, 256, 0, ctx->stream>>>(r.slot[ctx->cur], dst ? dst : ctx->d_staging, r.N, r.bs, r.nb,
+        gather_kernel<<<layout_grid(r.nb, r.bs), layout_threads(r.bs, ctx->nf), 0, ctx->stream>>>(r.slot[ctx->cur], dst ? dst : ctx->d_staging, r.N, r.bs, r.nb,
                                                          ctx->nf, store_of(ctx));
         ctx->launches++;
         CUDA_TRY(cudaGetLastError());
