@@ -309,6 +309,7 @@ __global__ void __launch_bounds__(96, 4) stage3_kernel(StageArgs a)
     const int lane = t & 31, warp = t >> 5;
     if (t < 128) sLed[t >> 5][t & 31] = 0.0f;
     const int slot0 = group_writer_slot<NF, 0>(lane);
+    float acc0[7] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};   // ledger group 0 of this pair, summed over rows
     const int slot1 = group_writer_slot<NF, 1>(lane);
     const int slot2 = group_writer_slot<NF, 2>(lane);
     const bool fake_on = P.fake_rate != 0.0f;
@@ -549,11 +550,9 @@ __global__ void __launch_bounds__(96, 4) stage3_kernel(StageArgs a)
                     uo[f] = o.hi;
                 }
                 if (up_ok) {   // the same row for the whole warp
-                    float v0[8];
+                    // group 0 (non-zero everywhere): the pair's running sums over the tile's rows
 #pragma unroll
-                    for (int m = 0; m < 8; ++m) v0[m] = led0[m];
-                    const float s0 = warp_sum_items<8>(v0, lane);
-                    if (slot0 >= 0) sLed[warp][slot0] += s0;
+                    for (int m = 0; m < 7; ++m) acc0[m] += led0[m];
                     if (sinks_any) {
                         float v1[8];
 #pragma unroll
@@ -601,6 +600,15 @@ __global__ void __launch_bounds__(96, 4) stage3_kernel(StageArgs a)
     }
 
     // ---- per-tile ledger and max speed (deterministic tree over the CTA) -------------
+    if (interior) {   // whole warps: group 0's column sums, one warp reduction per tile
+        float v0[8];
+#pragma unroll
+        for (int m = 0; m < 7; ++m) v0[m] = acc0[m];
+        v0[7] = 0.0f;
+        const float s0 = warp_sum_items<8>(v0, lane);
+        if (slot0 >= 0) sLed[warp][slot0] += s0;
+    }
+    __syncthreads();
     double* red = (double*)smem_raw;
     const int NT = blockDim.x;
     if (t < NL) {
