@@ -366,8 +366,8 @@ def ours(args):
                                          if ncu_traffic(args.workload, prec) else "no ncu capture of this workload",
                          "algorithmic_bytes_per_launch": bytes_per_launch,
                          "bytes_per_zone_update": bytes_per_zone_update, "stage_ms": stage_ms,
-                         "limiter": ("instruction issue and latency at 12 warps/SM (ncu: 49% issue active, "
-                                     "686 warp instructions per zone-stage, DRAM 17-24% of peak)")
+                         "limiter": ("instruction issue and latency at 12 warps/SM (ncu: 52% issue active, "
+                                     "676 warp instructions per zone-stage, DRAM 17-25% of peak)")
                                     if ncu_traffic(args.workload, prec) else "instruction issue (no ncu capture of this workload)"},
             "fp64": {"value": fp64_value, "ratio": (value / fp64_value) if fp64_value else None},
             "accuracy": accuracy,
