@@ -1,10 +1,15 @@
-"""One-orbit accuracy of the three precisions on the 2048² isothermal disk,
-against the CPU oracle.
+"""One-orbit accuracy of the three precisions against the CPU oracle, on the
+isothermal disk (2048², BASELINE config 2) or the Euler β-cooling disk
+(config 3, at a resolution the oracle can afford), and FP32 against FP64 on
+the GPU alone where the oracle cannot follow (config 5).
 
-Two steps, because the oracle's orbit costs about 8e10 zone-updates:
+Two steps, because the oracle's orbit costs up to 8e10 zone-updates:
 
     python tests/orbit_accuracy.py oracle --out tests/_cache/orbit2048.npz [--threads N]
     python tests/orbit_accuracy.py gpu --cache tests/_cache/orbit2048.npz [--json OUT]
+    (--workload euler --side 512 --fold 1 for the Euler disk, whose dt falls by
+    3.6x in its first steps: one dt for ten of them breaks the CFL condition)
+    python tests/orbit_accuracy.py compare --workload disk_8192 --steps 1000 [--json OUT]
 
 The first runs the oracle for one orbit (fold 10 advances until t >= 2π) and
 caches Σ at the end and the time series of the domain totals of the
@@ -32,9 +37,13 @@ FOLD = 10
 ITEMS = ("sink1", "sink2", "grav1", "grav2", "buffer", "cooling", "fake_mass")
 
 
-def _case(side):
+def _case(side, workload="disk"):
     import binary2d as b2
-    if side == 2048:
+    if workload == "euler":
+        mesh, hydro, physics, model = b2.presets.euler_beta_disk(side // 64, 64)
+    elif workload == "disk_8192":
+        mesh, hydro, physics, model = b2.presets.disk_8192()[:4]
+    elif side == 2048:
         mesh, hydro, physics, model = b2.presets.disk_2048(seed=1)
     else:
         mesh, hydro, physics, model = b2.presets.iso_disk(side // 64, 64, seed=1)
@@ -45,13 +54,13 @@ def _case(side):
 def run_oracle(args):
     import binary2d as b2
     from oracle import binding
-    mesh, hydro, physics, cons = _case(args.side)
+    mesh, hydro, physics, cons = _case(args.side, args.workload)
     st = binding.OracleState(b2.to_c(mesh, hydro, physics), cons)
     t_end = args.orbits * 2 * np.pi
     times, led, el, dts = [], [], [], []
     t0 = time.time()
     while st.time.value < t_end:
-        dts.append(st.advance(FOLD, nthreads=args.threads))
+        dts.append(st.advance(args.fold, nthreads=args.threads))
         times.append(st.time.value)
         led.append(st.ledger.sum(axis=(0, 1)))
         el.append(st.elements.sum(axis=(0, 1)))
@@ -60,7 +69,7 @@ def run_oracle(args):
     os.makedirs(os.path.dirname(os.path.abspath(args.out)), exist_ok=True)
     np.savez(args.out, sigma=st.cons[..., 0], times=np.array(times), ledger=np.array(led),
              elements=np.array(el), dts=np.array(dts), side=args.side, orbits=args.orbits,
-             seconds=time.time() - t0)
+             seconds=time.time() - t0, workload=args.workload, fold=args.fold)
     print("wrote %s: %d advances, t=%.6f, %.0f s" % (args.out, len(times), st.time.value, time.time() - t0))
 
 
@@ -68,10 +77,13 @@ def run_gpu(args):
     import binary2d as b2
     ref = np.load(args.cache)
     side = int(ref["side"])
-    mesh, hydro, physics, cons = _case(side)
+    workload = str(ref["workload"]) if "workload" in ref.files else "disk"
+    mesh, hydro, physics, cons = _case(side, workload)
     n = len(ref["times"])
+    fold = int(ref["fold"]) if "fold" in ref.files else FOLD
     sig_ref = ref["sigma"]
-    out = {"workload": "iso disk %d^2, one orbit" % side, "advances": n, "steps": n * FOLD,
+    out = {"workload": "%s %d^2, one orbit" % ("Euler beta-cooling disk" if workload == "euler" else "iso disk", side),
+           "advances": n, "steps": n * fold,
            "orbits": float(ref["times"][-1] / (2 * np.pi)),
            "oracle_seconds": float(ref["seconds"]), "precisions": {}}
     for p in ("fp64", "fp32_state64", "fp32_comp"):
@@ -81,7 +93,7 @@ def run_gpu(args):
             times, led, el = [], [], []
             t0 = time.time()
             for _ in range(n):
-                rt.advance(FOLD)
+                rt.advance(fold)
                 times.append(rt.time(0)[0])
                 led.append(rt.ledger(0).sum(axis=(0, 1)))
                 el.append(rt.elements(0).sum(axis=(0, 1)))
@@ -110,6 +122,36 @@ def run_gpu(args):
     print(json.dumps(out))
 
 
+def run_compare(args):
+    """FP32 paths against the FP64 GPU path after a fixed number of steps."""
+    import binary2d as b2
+    mesh, hydro, physics, cons = _case(0, args.workload)
+    n = args.steps // FOLD
+    res = {}
+    for p in ("fp64", "fp32_comp"):
+        with b2.Runtime([b2.Run(mesh, hydro, physics)], precision=p) as rt:
+            if p != "fp64":
+                rt.autotune()
+            rt.upload(0, cons)
+            t0 = time.time()
+            for _ in range(n):
+                rt.advance(FOLD)
+            s, t, _ = rt.download(0)
+            res[p] = (s[..., 0].copy(), rt.ledger(0).sum(axis=(0, 1)), t, time.time() - t0)
+        print(p, "done in %.1f s" % res[p][3], flush=True)
+    s64, l64, t64, _ = res["fp64"]
+    s32, l32, t32, _ = res["fp32_comp"]
+    acc64, acc32 = l64[0:2, 0].sum(), l32[0:2, 0].sum()
+    out = {"workload": args.workload, "steps": n * FOLD, "time_fp64": t64, "end_time_rel": abs(t32 - t64) / t64,
+           "l1_sigma_rel": float(np.abs(s32 - s64).sum() / np.abs(s64).sum()),
+           "accreted_mass_rel": float(abs(acc32 - acc64) / abs(acc64)) if acc64 else None,
+           "seconds": {"fp64": res["fp64"][3], "fp32_comp": res["fp32_comp"][3]}}
+    if args.json:
+        with open(args.json, "w") as f:
+            json.dump(out, f, indent=1)
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     sub = ap.add_subparsers(dest="cmd", required=True)
@@ -118,11 +160,17 @@ def main():
     o.add_argument("--side", type=int, default=2048)
     o.add_argument("--orbits", type=float, default=1.0)
     o.add_argument("--threads", type=int, default=None)
+    o.add_argument("--workload", default="disk", choices=["disk", "euler"])
+    o.add_argument("--fold", type=int, default=FOLD, help="RK steps per advance (one dt per advance)")
     g = sub.add_parser("gpu")
     g.add_argument("--cache", required=True)
     g.add_argument("--json", default="")
+    c = sub.add_parser("compare")
+    c.add_argument("--workload", default="disk_8192", choices=["disk_8192"])
+    c.add_argument("--steps", type=int, default=1000)
+    c.add_argument("--json", default="")
     args = ap.parse_args()
-    run_oracle(args) if args.cmd == "oracle" else run_gpu(args)
+    {"oracle": run_oracle, "gpu": run_gpu, "compare": run_compare}[args.cmd](args)
 
 
 if __name__ == "__main__":
