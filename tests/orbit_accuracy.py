@@ -101,10 +101,12 @@ def run_gpu(args):
             s, t, _ = rt.download(0)
         led, el = np.array(led), np.array(el)
         l1 = float(np.abs(s[..., 0] - sig_ref).sum() / np.abs(sig_ref).sum())
-        # per item and field: max over the series of |gpu - oracle| / max |oracle|
-        scale = np.maximum(np.abs(ref["ledger"]).max(axis=0), 1e-300)
+        # per item: max over the series and fields of |gpu - oracle|, divided by the
+        # item's largest |oracle| over the series and fields (a field that is zero up
+        # to rounding, such as cooling's momentum, is judged against its item)
+        scale = np.maximum(np.abs(ref["ledger"]).max(axis=(0, 2)), 1e-300)[:, None]
         led_err = (np.abs(led - ref["ledger"]).max(axis=0) / scale)
-        escale = np.maximum(np.abs(ref["elements"]).max(axis=0), 1e-300)
+        escale = np.maximum(np.abs(ref["elements"]).max(axis=(0, 2)), 1e-300)[:, None]
         el_err = (np.abs(el - ref["elements"]).max(axis=0) / escale)
         acc = ref["ledger"][-1, 0:2, 0].sum()
         out["precisions"][p] = {
