@@ -1039,7 +1039,16 @@ __global__ void tracer_kernel(const RunDev* runs, int run, int in_slot, int base
     const double R = rd.p.domain_radius, dx = rd.p.dx, dt = *rd.dt;
     const int N = rd.N;
     const double x = rd.tracers[in_slot][2 * k], y = rd.tracers[in_slot][2 * k + 1];
-    const double gx = (x + R) / dx - 0.5, gy = (y + R) / dx - 0.5;
+    // cell coordinates: the FP64 path divides as the oracle does; the FP32
+    // paths multiply by 1/dx (FP64 divisions are slow on this GPU)
+    double gx, gy;
+    if constexpr (std::is_same<T, double>::value) {
+        gx = (x + R) / dx - 0.5;
+        gy = (y + R) / dx - 0.5;
+    } else {
+        gx = (x + R) * rd.p.inv_dx - 0.5;
+        gy = (y + R) * rd.p.inv_dx - 0.5;
+    }
     const double fi = floor(gx), fj = floor(gy);
     const T ax = (T)(gx - fi), ay = (T)(gy - fj);
     int i0 = (int)fi, j0 = (int)fj;
