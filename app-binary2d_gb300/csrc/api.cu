@@ -1051,9 +1051,13 @@ __global__ void tracer_kernel(const RunDev* runs, int run, int in_slot, int base
     }
     const double fi = floor(gx), fj = floor(gy);
     const T ax = (T)(gx - fi), ay = (T)(gy - fj);
+    // positions are kept in [-R, R), so the cell index is in [-1, N - 1]: one
+    // conditional wrap, then a clamp that keeps any other input in bounds
     int i0 = (int)fi, j0 = (int)fj;
-    i0 = ((i0 % N) + N) % N;
-    j0 = ((j0 % N) + N) % N;
+    i0 = i0 < 0 ? i0 + N : i0;
+    j0 = j0 < 0 ? j0 + N : j0;
+    i0 = min(max(i0, 0), N - 1);
+    j0 = min(max(j0, 0), N - 1);
     const int i1 = i0 + 1 == N ? 0 : i0 + 1, j1 = j0 + 1 == N ? 0 : j0 + 1;
     T v00x, v00y, v10x, v10y, v01x, v01y, v11x, v11y;
     tracer_cell_velocity<T, STORE>(rd, in_slot, i0, j0, v00x, v00y);
