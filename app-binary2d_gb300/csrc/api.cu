@@ -1039,21 +1039,32 @@ __global__ void tracer_kernel(const RunDev* runs, int run, int in_slot, int base
     const double R = rd.p.domain_radius, dx = rd.p.dx, dt = *rd.dt;
     const int N = rd.N;
     const double x = rd.tracers[in_slot][2 * k], y = rd.tracers[in_slot][2 * k + 1];
-    // cell coordinates: the FP64 path divides as the oracle does; the FP32
-    // paths multiply by 1/dx (FP64 divisions are slow on this GPU)
-    double gx, gy;
+    const double L = 2.0 * R;
+    T ax, ay;
+    int i0, j0;
     if constexpr (std::is_same<T, double>::value) {
-        gx = (x + R) / dx - 0.5;
-        gy = (y + R) / dx - 0.5;
+        // the oracle's arithmetic
+        const double gx = (x + R) / dx - 0.5, gy = (y + R) / dx - 0.5;
+        const double fi = floor(gx), fj = floor(gy);
+        ax = gx - fi;
+        ay = gy - fj;
+        i0 = (int)fi;
+        j0 = (int)fj;
     } else {
-        gx = (x + R) * rd.p.inv_dx - 0.5;
-        gy = (y + R) * rd.p.inv_dx - 0.5;
+        // FP64 is slow on this GPU: the cell from an FP32 estimate, the offset in
+        // it exactly from FP64 (one fused step), then FP32 for the rest
+        const double xr = x + R, yr = y + R;
+        const float idx_f = (float)rd.p.inv_dx;
+        i0 = (int)floorf((float)xr * idx_f - 0.5f);
+        j0 = (int)floorf((float)yr * idx_f - 0.5f);
+        ax = (float)fma(-((double)i0 + 0.5), dx, xr) * idx_f;
+        ay = (float)fma(-((double)j0 + 0.5), dx, yr) * idx_f;
+        // the FP32 estimate can be one cell off within its rounding of a boundary
+        if (ax < 0.0f) { --i0; ax += 1.0f; } else if (ax >= 1.0f) { ++i0; ax -= 1.0f; }
+        if (ay < 0.0f) { --j0; ay += 1.0f; } else if (ay >= 1.0f) { ++j0; ay -= 1.0f; }
     }
-    const double fi = floor(gx), fj = floor(gy);
-    const T ax = (T)(gx - fi), ay = (T)(gy - fj);
     // positions are kept in [-R, R), so the cell index is in [-1, N - 1]: one
     // conditional wrap, then a clamp that keeps any other input in bounds
-    int i0 = (int)fi, j0 = (int)fj;
     i0 = i0 < 0 ? i0 + N : i0;
     j0 = j0 < 0 ? j0 + N : j0;
     i0 = min(max(i0, 0), N - 1);
@@ -1068,17 +1079,38 @@ __global__ void tracer_kernel(const RunDev* runs, int run, int in_slot, int base
     const T w00 = (one - ax) * (one - ay), w10 = ax * (one - ay), w01 = (one - ax) * ay, w11 = ax * ay;
     const T vx = w00 * v00x + w10 * v10x + w01 * v01x + w11 * v11x;
     const T vy = w00 * v00y + w10 * v10y + w01 * v01y + w11 * v11y;
-    double xo = x + dt * (double)vx, yo = y + dt * (double)vy;
-    const double L = 2.0 * R;
-    if (base_slot >= 0) {
-        // average with the base position on the same periodic image
-        const double xb = rd.tracers[base_slot][2 * k], yb = rd.tracers[base_slot][2 * k + 1];
-        if (xo - xb > R) xo -= L;
-        else if (xo - xb < -R) xo += L;
-        if (yo - yb > R) yo -= L;
-        else if (yo - yb < -R) yo += L;
-        xo = xo * (-bf + 1.0) + xb * bf;
-        yo = yo * (-bf + 1.0) + yb * bf;
+    double xo, yo;
+    if constexpr (std::is_same<T, double>::value) {
+        xo = x + dt * vx;
+        yo = y + dt * vy;
+        if (base_slot >= 0) {
+            // average with the base position on the same periodic image
+            const double xb = rd.tracers[base_slot][2 * k], yb = rd.tracers[base_slot][2 * k + 1];
+            if (xo - xb > R) xo -= L;
+            else if (xo - xb < -R) xo += L;
+            if (yo - yb > R) yo -= L;
+            else if (yo - yb < -R) yo += L;
+            xo = xo * (-bf + 1.0) + xb * bf;
+            yo = yo * (-bf + 1.0) + yb * bf;
+        }
+    } else {
+        // the stage's displacement in FP32, accumulated in FP64
+        const float dtf = (float)dt;
+        xo = x + (double)(dtf * vx);
+        yo = y + (double)(dtf * vy);
+        if (base_slot >= 0) {
+            // base + (new - base) (1 - bf), on the base's periodic image
+            const double xb = rd.tracers[base_slot][2 * k], yb = rd.tracers[base_slot][2 * k + 1];
+            double ddx = xo - xb, ddy = yo - yb;
+            const float Rf = (float)R;
+            if ((float)ddx > Rf) ddx -= L;
+            else if ((float)ddx < -Rf) ddx += L;
+            if ((float)ddy > Rf) ddy -= L;
+            else if ((float)ddy < -Rf) ddy += L;
+            const double w1 = -bf + 1.0;
+            xo = fma(ddx, w1, xb);
+            yo = fma(ddy, w1, yb);
+        }
     }
     if (xo >= R) xo -= L;
     if (xo < -R) xo += L;
