@@ -74,6 +74,8 @@ _SIGNATURES = [
     ("b2d_max_signal_speed", c_int32, [ctypes.c_void_p, c_int32, c_dp]),
     ("b2d_initial_state", c_int32, [ctypes.POINTER(B2DConfig), ctypes.POINTER(B2DDiskModel), c_dp]),
     ("b2d_set_tile", c_int32, [ctypes.c_void_p, c_int32, c_int32]),
+    ("b2d_set_strip_rows", c_int32, [ctypes.c_void_p, c_int32]),
+    ("b2d_get_strip_rows", c_int32, [ctypes.c_void_p, ctypes.POINTER(c_int32)]),
     ("b2d_get_tile", c_int32, [ctypes.c_void_p, ctypes.POINTER(c_int32), ctypes.POINTER(c_int32)]),
     ("b2d_set_graphs", c_int32, [ctypes.c_void_p, c_int32]),
     ("b2d_launch_count", c_int64, [ctypes.c_void_p]),

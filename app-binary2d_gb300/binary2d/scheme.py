@@ -234,6 +234,16 @@ class Runtime:
         _check(self.lib.b2d_get_tile(self.ctx, ctypes.byref(w), ctypes.byref(h)))
         return w.value, h.value
 
+    def set_strip_rows(self, rows: int = 0):
+        """Row chunks of at most `rows` rows, crossing block boundaries, for the
+        paired FP32 kernel (0: block-aligned tiles of the tile height)."""
+        _check(self.lib.b2d_set_strip_rows(self.ctx, int(rows)))
+
+    def strip_rows(self) -> int:
+        r = ctypes.c_int32(0)
+        _check(self.lib.b2d_get_strip_rows(self.ctx, ctypes.byref(r)))
+        return r.value
+
     def autotune(self, fold: int = 2, reps: int = 2):
         """Pick the fastest tile shape for this context; returns (w, h, ms/stage)."""
         w, h, ms = ctypes.c_int32(0), ctypes.c_int32(0), ctypes.c_double(0)

@@ -20,6 +20,7 @@
 namespace b2d {
 cudaError_t launch_stage_f64(int nf, const StageArgs& a, int grid, int tw, size_t smem, cudaStream_t s);
 cudaError_t launch_stage_f32(int nf, int store, const StageArgs& a, int grid, int tw, size_t smem, cudaStream_t s);
+int paired_ctas_per_sm(int nruns, int tw);
 void host_block_vertices(const b2d_config* c, int b, double* xv);
 void host_cell_centers(const b2d_config* c, int b, double* xc);
 }  // namespace b2d
@@ -230,7 +231,7 @@ struct RunHost {
     double* partial = nullptr;
     unsigned* counter = nullptr;
     double *xc = nullptr, *xv = nullptr;
-    float *xcf = nullptr, *xvf = nullptr;
+    float *xcf = nullptr, *xvf = nullptr, *xvgf = nullptr;
     double* stage_time = nullptr;
     double* orbit = nullptr;
     double* stage_ds = nullptr;
@@ -254,6 +255,7 @@ struct StagePlan {
 struct b2d_ctx {
     int nruns = 0, nf = 3, precision = 0, hydro = 0, rk = 2;
     int tw = 64, th = 64;
+    int strip_rows = 0;   // > 0: the paired FP32 kernel covers column strips in row chunks of at most this many rows
     int cur = 0;
     std::vector<RunHost> runs;
     std::vector<RunDev> rdev_h;
@@ -408,7 +410,7 @@ static void free_ctx(b2d_ctx* ctx)
         if (ri < ctx->rdev_h.size())
             for (int s = 0; s < NSLOTS; ++s) cudaFree(ctx->rdev_h[ri].tracers[s]);
         cudaFree(r.bg); cudaFree(r.partial); cudaFree(r.counter);
-        cudaFree(r.xc); cudaFree(r.xv); cudaFree(r.xcf); cudaFree(r.xvf);
+        cudaFree(r.xc); cudaFree(r.xv); cudaFree(r.xcf); cudaFree(r.xvf); cudaFree(r.xvgf);
         cudaFree(r.stage_time); cudaFree(r.orbit); cudaFree(r.stage_ds); cudaFree(r.stage_de);
     }
     cudaFree(ctx->rdev); cudaFree(ctx->d_dt); cudaFree(ctx->d_time); cudaFree(ctx->d_iter);
@@ -428,17 +430,37 @@ static void free_ctx(b2d_ctx* ctx)
 
 // Rebuild the tile bookkeeping for the current tile shape and push the run
 // descriptors to the device.
+// The stage kernel the context launches is the paired-column FP32 kernel
+// (launch_stage_f32 makes the same choice).
+static bool paired_kernel(const b2d_ctx* ctx)
+{
+    return ctx->precision == B2D_PREC_FP32_COMP && ctx->nf == 3 && ctx->tw % 64 == 0 && ctx->tw <= 128;
+}
+
+// Row chunks per column strip of a run: block-aligned tiles of height th, or,
+// with strip rows set and the paired kernel launched, ceil(N / rows) chunks
+// that may cross one block boundary each.
+static int row_chunks(const b2d_ctx* ctx, const RunHost& r)
+{
+    if (ctx->strip_rows > 0 && paired_kernel(ctx)) return (r.N + ctx->strip_rows - 1) / ctx->strip_rows;
+    return r.N / ctx->th;
+}
+
 static b2d_status sync_rundev(b2d_ctx* ctx)
 {
     int base = 0;
     for (int i = 0; i < ctx->nruns; ++i) {
         RunHost& r = ctx->runs[i];
         RunDev& d = ctx->rdev_h[i];
-        d.tiles_i = r.N / ctx->th;
+        d.tiles_i = row_chunks(ctx, r);
         d.tiles_j = r.N / ctx->tw;
         d.ntiles = d.tiles_i * d.tiles_j;
         d.tile_base = base;
-        d.tiles_per_block = (r.bs / ctx->th) * (r.bs / ctx->tw);
+        // partial slots of the block with the most chunk pieces (every block:
+        // bs / th for block-aligned tiles)
+        int most = 0;
+        for (int b = 0; b < r.nb; ++b) most = std::max(most, chunks_in_block_row(b, r.bs, r.N, d.tiles_i));
+        d.tiles_per_block = most * (r.bs / ctx->tw);
         base += d.ntiles;
         CUDA_TRY(cudaFree(r.partial));
         r.partial = nullptr;
@@ -568,18 +590,24 @@ extern "C" b2d_ctx* b2d_create(const b2d_config* cfgs, int32_t nruns, int32_t pr
             host_block_vertices(&cfgs[i], b, xv.data() + (size_t)b * (r.bs + 1));
         }
         std::vector<float> xcf(xc.begin(), xc.end()), xvf(xv.begin(), xv.end());
+        // row faces by global index: face k of block k / bs, the last block's top face last
+        std::vector<float> xvgf((size_t)r.N + 1);
+        for (int k = 0; k < r.N; ++k) xvgf[k] = xvf[(size_t)(k / r.bs) * (r.bs + 1) + k % r.bs];
+        xvgf[r.N] = xvf[(size_t)(r.nb - 1) * (r.bs + 1) + r.bs];
         r.hxc = xc;
         CREATE_TRY(cudaMalloc(&r.xc, sizeof(double) * xc.size()));
         CREATE_TRY(cudaMalloc(&r.xv, sizeof(double) * xv.size()));
         CREATE_TRY(cudaMalloc(&r.xcf, sizeof(float) * xc.size()));
         CREATE_TRY(cudaMalloc(&r.xvf, sizeof(float) * xv.size()));
+        CREATE_TRY(cudaMalloc(&r.xvgf, sizeof(float) * xvgf.size()));
         CREATE_TRY(cudaMemcpy(r.xc, xc.data(), sizeof(double) * xc.size(), cudaMemcpyHostToDevice));
         CREATE_TRY(cudaMemcpy(r.xv, xv.data(), sizeof(double) * xv.size(), cudaMemcpyHostToDevice));
         CREATE_TRY(cudaMemcpy(r.xcf, xcf.data(), sizeof(float) * xc.size(), cudaMemcpyHostToDevice));
         CREATE_TRY(cudaMemcpy(r.xvf, xvf.data(), sizeof(float) * xv.size(), cudaMemcpyHostToDevice));
+        CREATE_TRY(cudaMemcpy(r.xvgf, xvgf.data(), sizeof(float) * xvgf.size(), cudaMemcpyHostToDevice));
 
         d.N = r.N; d.bs = r.bs; d.nb = r.nb; d.nblocks = r.nblocks;
-        d.xc = r.xc; d.xv = r.xv; d.xcf = r.xcf; d.xvf = r.xvf;
+        d.xc = r.xc; d.xv = r.xv; d.xcf = r.xcf; d.xvf = r.xvf; d.xvgf = r.xvgf;
         for (int s = 0; s < NSLOTS; ++s) {
             d.slot[s] = r.slot[s];
             d.ledger[s] = r.ledger[s];
@@ -1406,6 +1434,26 @@ extern "C" b2d_status b2d_get_tile(const b2d_ctx* ctx, int32_t* tile_w, int32_t*
     return B2D_OK;
 }
 
+extern "C" b2d_status b2d_set_strip_rows(b2d_ctx* ctx, int32_t rows)
+{
+    if (!ctx || rows < 0) return fail(B2D_ERR_INVALID, "bad arguments");
+    if (rows > 0) {
+        if (rows < 8) return fail(B2D_ERR_INVALID, "strip rows must be 0 or at least 8");
+        for (const RunHost& r : ctx->runs)
+            if (rows > r.bs) return fail(B2D_ERR_INVALID, "strip rows must not exceed the block size");
+    }
+    CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    ctx->strip_rows = rows;
+    return sync_rundev(ctx);
+}
+
+extern "C" b2d_status b2d_get_strip_rows(const b2d_ctx* ctx, int32_t* rows)
+{
+    if (!ctx || !rows) return fail(B2D_ERR_INVALID, "bad arguments");
+    *rows = ctx->strip_rows;
+    return B2D_OK;
+}
+
 extern "C" b2d_status b2d_set_graphs(b2d_ctx* ctx, int32_t enable)
 {
     if (!ctx) return fail(B2D_ERR_INVALID, "bad arguments");
@@ -1510,6 +1558,34 @@ static b2d_status time_tile(b2d_ctx* ctx, int fold, int reps, double* ms)
     return B2D_OK;
 }
 
+// Strip rows for the paired kernel at the context's tile width: for the
+// fewest whole waves of resident CTAs that chunks of at most a block's rows
+// fill, and the next two, the shortest chunks that still fit in them.
+static std::vector<int> strip_row_candidates(const b2d_ctx* ctx)
+{
+    std::vector<int> out;
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return out;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return out;
+    const int per_sm = paired_ctas_per_sm(ctx->nruns, ctx->tw);
+    if (sms <= 0 || per_sm <= 0) return out;
+    const long long slots = (long long)sms * per_sm;
+    int min_bs = 1 << 30;
+    for (const RunHost& r : ctx->runs) min_bs = std::min(min_bs, r.bs);
+    auto ctas = [&](int rows) {
+        long long n = 0;
+        for (const RunHost& r : ctx->runs) n += (long long)((r.N + rows - 1) / rows) * (r.N / ctx->tw);
+        return n;
+    };
+    long long waves = (ctas(min_bs) + slots - 1) / slots;
+    for (int c = 0; c < 3; ++c, ++waves) {
+        int best = 0;
+        for (int rows = min_bs; rows >= 8 && ctas(rows) <= waves * slots; --rows) best = rows;
+        if (best && std::find(out.begin(), out.end(), best) == out.end()) out.push_back(best);
+    }
+    return out;
+}
+
 extern "C" b2d_status b2d_autotune(b2d_ctx* ctx, int32_t fold, int32_t reps, int32_t* tile_w, int32_t* tile_h,
                                    double* ms_per_stage)
 {
@@ -1518,8 +1594,9 @@ extern "C" b2d_status b2d_autotune(b2d_ctx* ctx, int32_t fold, int32_t reps, int
     if (st != B2D_OK) return st;
     CUDA_TRY(cudaStreamSynchronize(ctx->stream));
     const int max_w = ctx->precision == B2D_PREC_FP64 ? 256 : 128;
-    int best_w = ctx->tw, best_h = ctx->th;
+    int best_w = ctx->tw, best_h = ctx->th, best_rows = 0;
     double best = 1e300;
+    ctx->strip_rows = 0;
     for (int w : {32, 64, 128, 256}) {
         if (w > max_w) continue;
         for (int h : {8, 16, 32, 64, 128}) {
@@ -1534,6 +1611,26 @@ extern "C" b2d_status b2d_autotune(b2d_ctx* ctx, int32_t fold, int32_t reps, int
             if (ms < best) { best = ms; best_w = w; best_h = h; }
         }
     }
+    // row chunks of the paired kernel, at both of its tile widths
+    for (int w : {64, 128}) {
+        int h = 0;
+        for (int hh : {64, 32, 16, 8})
+            if (!h && tile_ok(ctx, w, hh)) h = hh;
+        if (!h) continue;
+        ctx->tw = w;
+        ctx->th = h;
+        if (!paired_kernel(ctx)) continue;
+        for (int rows : strip_row_candidates(ctx)) {
+            ctx->strip_rows = rows;
+            st = sync_rundev(ctx);
+            if (st != B2D_OK) return st;
+            double ms = 0;
+            st = time_tile(ctx, fold, reps, &ms);
+            if (st != B2D_OK) return st;
+            if (ms < best) { best = ms; best_w = w; best_h = h; best_rows = rows; }
+        }
+        ctx->strip_rows = 0;
+    }
     // discard what the trial advances left behind
     long long count = 0;
     CUDA_TRY(cudaMemcpy(&count, ctx->d_adv_count, sizeof count, cudaMemcpyDeviceToHost));
@@ -1543,6 +1640,7 @@ extern "C" b2d_status b2d_autotune(b2d_ctx* ctx, int32_t fold, int32_t reps, int
     CUDA_TRY(cudaMemset(ctx->d_timeout, 0, sizeof(unsigned)));
     ctx->tw = best_w;
     ctx->th = best_h;
+    ctx->strip_rows = best_rows;
     st = sync_rundev(ctx);
     if (st != B2D_OK) return st;
     for (int r = 0; r < ctx->nruns; ++r) {

@@ -48,6 +48,18 @@ static cudaError_t launch_three_impl(const StageArgs& a, int grid, int tw, cudaS
     return cudaGetLastError();
 }
 
+// Resident CTAs per SM of the paired kernel for a tile width (the autotuner
+// sizes row chunks to whole waves with it).
+int paired_ctas_per_sm(int nruns, int tw)
+{
+    const size_t smem = s3_smem_bytes(tw);
+    int n = 0;
+    cudaError_t e = nruns == 1
+        ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, stage3_kernel<true>, tw / 2 + 32, smem)
+        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, stage3_kernel<false>, tw / 2 + 32, smem);
+    return e == cudaSuccess ? n : 0;
+}
+
 cudaError_t launch_stage_f32(int nf, int store, const StageArgs& a, int grid, int tw, size_t smem, cudaStream_t s)
 {
     if (nf == 3 && store == 1 && tw % 64 == 0 && tw <= 128)

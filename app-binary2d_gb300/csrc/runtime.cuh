@@ -19,6 +19,7 @@ struct RunDev {
     const double* xv;        // [nb][bs+1] block vertices (mesh.rs:42-47)
     const float* xcf;
     const float* xvf;
+    const float* xvgf;       // [N+1] row faces by global index, FP32 (a block's first vertex at its lower boundary)
     void* slot[NSLOTS];      // conserved state per slot (STORE layout)
     const void* bg;          // BlockData::initial_conserved (STORE layout)
     double* ledger[NSLOTS];  // [nblocks][7][nf] per slot
@@ -54,6 +55,24 @@ struct StageArgs {
     unsigned long long* err_key;  // failure key, ~0 when no zone failed
     unsigned* timeout_flag;       // set when a bounded wait gave up
 };
+
+// Row chunks of a column strip.  A run's N rows split into C chunks; chunk c
+// covers rows [c N / C, (c + 1) N / C).  With C = N / th the chunks are the
+// block-aligned tiles of height th; with C = ceil(N / rows) for rows <= bs a
+// chunk crosses at most one block boundary.  C <= N and N^2 <= 2^31 (the
+// mesh limit of validate, api.cu) keep c N and (r + 1) C below 2^32, so
+// 32-bit unsigned arithmetic is exact (a 64-bit division costs the stage
+// kernel about a thousand instructions).
+__host__ __device__ inline int chunk_start(int c, int N, int C) { return (int)((unsigned)c * (unsigned)N / (unsigned)C); }
+__host__ __device__ inline int chunk_of_row(int r, int N, int C)
+{
+    return (int)((((unsigned)r + 1u) * (unsigned)C - 1u) / (unsigned)N);
+}
+// chunks that cover rows of block row b (bs rows from b bs)
+__host__ __device__ inline int chunks_in_block_row(int b, int bs, int N, int C)
+{
+    return chunk_of_row((b + 1) * bs - 1, N, C) - chunk_of_row(b * bs, N, C) + 1;
+}
 
 template <class R> __host__ __device__ inline const DevParamsT<R>& params_of(const RunDev& rd);
 template <> __host__ __device__ inline const DevParamsT<double>& params_of<double>(const RunDev& rd) { return rd.p; }

@@ -645,6 +645,7 @@ __global__ void __launch_bounds__(160, (NF == 3 && STORE == 1) ? 4 : 3) stage2_k
         if (live)
             for (int w = 0; w < TW / 32; ++w) s += (double)sLed[w][j];
         rd.partial[((size_t)block * rd.tiles_per_block + tib) * NL + t] = s;
+        __threadfence();   // visible before the counter below counts this tile
     }
     if (a.amax_flag) {
         red[t] = (double)amax;
@@ -658,6 +659,7 @@ __global__ void __launch_bounds__(160, (NF == 3 && STORE == 1) ? 4 : 3) stage2_k
     if (t == 0 && timeout) atomicOr(a.timeout_flag, 1u);
 
     __shared__ int is_last;
+    __syncthreads();
     if (t == 0) {
         __threadfence();
         unsigned prev = atomicAdd(rd.counter + block, 1u);

@@ -23,6 +23,15 @@
 //    the tile's right face) and the TMA producer on lane 4.  The halo lanes'
 //    outer columns (-2 and TW+1) need stencil points outside the staged halo;
 //    they read clamped in-bounds values and their results are never used.
+//  * Row chunks.  A tile is a column strip's row chunk (chunk_start,
+//    runtime.cuh).  Chunks may cross one block boundary, so that the number of
+//    CTAs can be a whole number of waves (a CTA's time is set by its row chain,
+//    not by how many CTAs share its SM).  The source ledger of a crossing
+//    tile's rows in its first block row is reduced into a second shared bank
+//    when the last of them is updated (one warp-uniform branch in the row
+//    loop); after the loop warp 0 writes the main piece and the halo warp the
+//    first, at once; a block's pieces are folded by its last piece, in piece
+//    order.
 #pragma once
 
 #include "stage2.cuh"
@@ -159,6 +168,68 @@ __host__ __device__ inline int s3_smem_bytes(int tw)
     return slots + exch + 8 * (S3_SLOTS + S3_USLOTS);
 }
 
+// One ledger piece of a tile (its rows in block row brow), by one warp after
+// the row loop: sums over the interior warps' bank rows, the piece's slot in
+// the block's partials, and the fold of the block's pieces (in piece order)
+// by the block's last piece.  acc (a crossing tile's first piece) holds group
+// 0 per thread, to be reduced here first.  Out of line, so that it does not
+// weigh on the row loop's register allocation; no CTA barrier, so that two
+// warps can flush two pieces at once.
+template <int NF>
+__device__ __noinline__ void flush_piece(const RunDev& rd, int brow, int bj, int lslot, int TW, float (*bank)[32],
+                                         const float (*acc)[64], int in_slot, int base_slot, int out_slot,
+                                         int stage, double bf)
+{
+    constexpr int NL = NITEMS * NF;
+    const int lane = threadIdx.x & 31, TP = TW / 2;
+    if (acc) {
+        float v0[8];
+#pragma unroll
+        for (int m = 0; m < 7; ++m) v0[m] = acc[m][lane] + (TP > 32 ? acc[m][lane + 32] : 0.0f);
+        v0[7] = 0.0f;
+        const float s0 = warp_sum_items<8>(v0, lane);
+        const int slot0 = group_writer_slot<NF, 0>(lane);
+        if (slot0 >= 0) bank[0][slot0] += s0;
+        __syncwarp();
+    }
+    const int bs = rd.bs, nc = rd.tiles_i, per_row = bs / TW;
+    const int ti = ((int)blockIdx.x - rd.tile_base) / rd.tiles_j;
+    const int block = brow * rd.nb + bj;
+    const int piece = (ti - chunk_of_row(brow * bs, rd.N, nc)) * per_row + lslot;
+    const int pieces = chunks_in_block_row(brow, bs, rd.N, nc) * per_row;
+    if (lane < NL) {
+        int j = 0;
+        bool live = false;
+        for (int k2 = 0; k2 < NL; ++k2) {
+            if (k2 == lane) { live = item_live<NF>(k2); break; }
+            if (item_live<NF>(k2)) ++j;
+        }
+        double s = 0.0;
+        if (live)
+            for (int w = 0; w < TP / 32; ++w) s += (double)bank[w][j];
+        rd.partial[((size_t)block * rd.tiles_per_block + piece) * NL + lane] = s;
+        __threadfence();   // visible before the counter below counts this piece
+    }
+    __syncwarp();
+    unsigned last = 0;
+    if (lane == 0) last = atomicAdd(rd.counter + block, 1u) == (unsigned)pieces - 1;
+    last = __shfl_sync(0xffffffffu, last, 0);
+    if (!last) return;
+    __threadfence();
+    if (lane < NL) {
+        const double area = (double)rd.p.dx * rd.p.dx;
+        double s = 0.0;
+        for (int q = 0; q < pieces; ++q)
+            s += __ldcg(rd.partial + ((size_t)block * rd.tiles_per_block + q) * NL + lane);
+        double v = __ldcg(rd.ledger[in_slot] + (size_t)block * NL + lane) + s * area;
+        if (base_slot >= 0) v = v * (-bf + 1.0) + __ldcg(rd.ledger[base_slot] + (size_t)block * NL + lane) * bf;
+        rd.ledger[out_slot][(size_t)block * NL + lane] = v;
+        // the block's ds·dx·dy of this stage, for the orbital-element ledger
+        if (rd.stage_ds) rd.stage_ds[((size_t)stage * rd.nblocks + block) * NL + lane] = s * area;
+    }
+    if (lane == 0) rd.counter[block] = 0u;
+}
+
 template <bool SINGLE>
 __global__ void __launch_bounds__(96, 4) stage3_kernel(StageArgs a)
 {
@@ -168,7 +239,6 @@ __global__ void __launch_bounds__(96, 4) stage3_kernel(StageArgs a)
 
     const int TP = blockDim.x - 32;          // interior threads (column pairs)
     const int TW = 2 * TP;
-    const int TH = a.th;
     const int t = threadIdx.x;
     const int SW = TW + 2 * H;
 
@@ -201,10 +271,16 @@ __global__ void __launch_bounds__(96, 4) stage3_kernel(StageArgs a)
     const size_t nn = (size_t)N * N;
     const int lt = g - rd.tile_base;
     const int tj = lt % rd.tiles_j, ti = lt / rd.tiles_j;
-    const int i0 = ti * TH, j0 = tj * TW;
-    const int bi = i0 / bs, bj = j0 / bs, li0 = i0 % bs, lj0 = j0 % bs;
-    const int block = bi * rd.nb + bj;
-    const int tib = (li0 / TH) * (bs / TW) + lj0 / TW;
+    // rows [i0, i0 + TH) of the column strip from j0: row chunk ti of C.  A chunk
+    // of at most bs rows lies in one block row, or in two from its row rb; the
+    // ledger piece of the last block row is the tile's main piece
+    const int C = rd.tiles_i;
+    const int i0 = chunk_start(ti, N, C), TH = chunk_start(ti + 1, N, C) - i0, j0 = tj * TW;
+    const int bj = j0 / bs, lj0 = j0 % bs;
+    const int rb = min(bs - i0 % bs, TH);
+    const int bl = (i0 + TH - 1) / bs;
+    const int block = bl * rd.nb + bj;
+    const int tib = (ti - chunk_of_row(bl * bs, N, C)) * (bs / TW) + lj0 / TW;
     const bool has_base = a.base_slot >= 0;
 
     const float* uin = (const float*)rd.slot[a.in_slot];
@@ -291,7 +367,7 @@ __global__ void __launch_bounds__(96, 4) stage3_kernel(StageArgs a)
     const float2 yc2 = interior ? make_float2(xc[j0 + c0], xc[j0 + c0 + 1]) : f2(0.0f);
     const int fv = bj * (bs + 1) + lj0;
     const float2 yv2 = (interior || hl == 1) ? make_float2(xv[fv + c0], xv[fv + min(c0 + 1, TW)]) : f2(0.0f);
-    const float* xv_row = xv + bi * (bs + 1) + li0;
+    const float* xv_row = rd.xvgf + i0;
     const float* xc_row = xc + i0;
     // dy^2 + s^2 of a pair of y positions to each body (recomputed where used:
     // registers are the scarcer resource here)
@@ -305,9 +381,11 @@ __global__ void __launch_bounds__(96, 4) stage3_kernel(StageArgs a)
     float2 xg[NF], xtn = f2(0.0f), xtt = f2(0.0f);   // row rg's x slopes and stresses, for this row's x faces
     constexpr int NLIVE = live_items<NF>();
     static_assert(group_size<NF, 0>() + group_size<NF, 1>() + group_size<NF, 2>() == NLIVE, "ledger groups");
-    __shared__ float sLed[4][32];
+    // [warp][item slot] of the main piece and of a crossing tile's first piece;
+    // group 0 of the first piece per thread
+    __shared__ float sLed[4][32], sLedA[4][32], sAccA[7][64];
     const int lane = t & 31, warp = t >> 5;
-    if (t < 128) sLed[t >> 5][t & 31] = 0.0f;
+    if (t < 128) sLed[t >> 5][t & 31] = sLedA[t >> 5][t & 31] = 0.0f;
     const int slot0 = group_writer_slot<NF, 0>(lane);
     float acc0[7] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};   // ledger group 0 of this pair, summed over rows
     const int slot1 = group_writer_slot<NF, 1>(lane);
@@ -569,6 +647,13 @@ __global__ void __launch_bounds__(96, 4) stage3_kernel(StageArgs a)
                         const float s2 = warp_sum_items<4>(v2, lane);
                         if (slot2 >= 0) sLed[warp][slot2] += s2;
                     }
+                    if (ru == rb - 1 && rb < TH) {   // the first piece's last row: set its sums aside
+                        __syncwarp();
+                        sLedA[warp][lane] = sLed[warp][lane];
+                        sLed[warp][lane] = 0.0f;
+#pragma unroll
+                        for (int m = 0; m < 7; ++m) { sAccA[m][t] = acc0[m]; acc0[m] = 0.0f; }
+                    }
                 }
                 if (want_amax && up_ok) {
                     const float ua[NF] = {uo[0].x, uo[1].x, uo[2].x}, ub[NF] = {uo[0].y, uo[1].y, uo[2].y};
@@ -599,30 +684,9 @@ __global__ void __launch_bounds__(96, 4) stage3_kernel(StageArgs a)
         __syncthreads();
     }
 
-    // ---- per-tile ledger and max speed (deterministic tree over the CTA) -------------
-    if (interior) {   // whole warps: group 0's column sums, one warp reduction per tile
-        float v0[8];
-#pragma unroll
-        for (int m = 0; m < 7; ++m) v0[m] = acc0[m];
-        v0[7] = 0.0f;
-        const float s0 = warp_sum_items<8>(v0, lane);
-        if (slot0 >= 0) sLed[warp][slot0] += s0;
-    }
-    __syncthreads();
+    // ---- max speed of the tile (deterministic tree over the CTA; the ring is idle) --
     double* red = (double*)smem_raw;
     const int NT = blockDim.x;
-    if (t < NL) {
-        int j = 0;
-        bool live = false;
-        for (int k2 = 0; k2 < NL; ++k2) {
-            if (k2 == t) { live = item_live<NF>(k2); break; }
-            if (item_live<NF>(k2)) ++j;
-        }
-        double s = 0.0;
-        if (live)
-            for (int w = 0; w < TP / 32; ++w) s += (double)sLed[w][j];
-        rd.partial[((size_t)block * rd.tiles_per_block + tib) * NL + t] = s;
-    }
     if (a.amax_flag) {
         red[t] = (double)amax;
         __syncthreads();
@@ -634,31 +698,24 @@ __global__ void __launch_bounds__(96, 4) stage3_kernel(StageArgs a)
     }
     if (t == 0 && timeout) atomicOr(a.timeout_flag, 1u);
 
-    __shared__ int is_last;
-    if (t == 0) {
-        __threadfence();
-        unsigned prev = atomicAdd(rd.counter + block, 1u);
-        is_last = (prev == (unsigned)rd.tiles_per_block - 1);
+    // ---- ledger pieces: the main piece by warp 0 and a crossing tile's first piece
+    // (the block row above) by the halo warp, at once ------------------------------
+    if (interior) {   // whole warps: group 0's column sums, one warp reduction per tile
+        float v0[8];
+#pragma unroll
+        for (int m = 0; m < 7; ++m) v0[m] = acc0[m];
+        v0[7] = 0.0f;
+        const float s0 = warp_sum_items<8>(v0, lane);
+        if (slot0 >= 0) sLed[warp][slot0] += s0;
     }
     __syncthreads();
-    if (is_last) {
-        __threadfence();
-        const double area = (double)rd.p.dx * rd.p.dx;
-        const double* lin = rd.ledger[a.in_slot] + (size_t)block * NL;
-        const double* lbase = has_base ? rd.ledger[a.base_slot] + (size_t)block * NL : nullptr;
-        double* lout = rd.ledger[a.out_slot] + (size_t)block * NL;
-        for (int k = t; k < NL; k += NT) {
-            double s = 0.0;
-            for (int q = 0; q < rd.tiles_per_block; ++q)
-                s += __ldcg(rd.partial + ((size_t)block * rd.tiles_per_block + q) * NL + k);
-            double v = __ldcg(lin + k) + s * area;
-            if (lbase) v = v * (-a.bf + 1.0) + __ldcg(lbase + k) * a.bf;
-            lout[k] = v;
-            // the block's ds·dx·dy of this stage, for the orbital-element ledger
-            if (rd.stage_ds) rd.stage_ds[((size_t)a.stage * rd.nblocks + block) * NL + k] = s * area;
-        }
-        if (t == 0) rd.counter[block] = 0u;
-    }
+    const int brow = block / rd.nb, lslot = tib % (rd.bs / TW);
+    if (warp == 0)
+        flush_piece<NF>(rd, brow, block - brow * rd.nb, lslot, TW, sLed, nullptr, a.in_slot, a.base_slot, a.out_slot,
+                        a.stage, a.bf);
+    else if (warp == TP / 32 && rb < TH)
+        flush_piece<NF>(rd, brow - 1, block - brow * rd.nb, lslot, TW, sLedA, sAccA, a.in_slot, a.base_slot,
+                        a.out_slot, a.stage, a.bf);
 }
 
 }  // namespace b2d

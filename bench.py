@@ -227,11 +227,14 @@ def ours(args):
             rt.set_tracers(0, tracers)
         if args.tile:
             rt.set_tile(*[int(x) for x in args.tile.split("x")])
+            rt.set_strip_rows(max(args.strip_rows, 0))
+            tuned[prec] = rt.tile() + (rt.strip_rows(),)
         elif prec in tuned:
-            rt.set_tile(*tuned[prec])
+            rt.set_tile(*tuned[prec][:2])
+            rt.set_strip_rows(tuned[prec][2])
         else:
             w, h, _ = rt.autotune(fold=2, reps=2)
-            tuned[prec] = (w, h)
+            tuned[prec] = (w, h, rt.strip_rows())
         return rt
 
     def barrier():
@@ -358,7 +361,8 @@ def ours(args):
                        "tracer_bytes_per_step": (2 * 32 * FOLD * int(args.tracers)) if tracers is not None else 0,
                        "global_batch": ws, "parallelism": "replicas" if ws > 1 else "single GPU",
                        "l2": "state + background > L2 (no flush needed)",
-                       "tile": "%dx%d" % tuned.get(prec, (0, 0)) if not args.tile else args.tile,
+                       "tile": "%dx%d" % tuned.get(prec, (0, 0, 0))[:2],
+                       "strip_rows": tuned.get(prec, (0, 0, 0))[2],
                        "tile_source": "autotuner" if not args.tile else "--tile"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                          "frac": achieved / hbm_peak, "peak_kind": peak_kind,
@@ -404,6 +408,7 @@ def sweep_bench(args, torch, b2, ws, rank, dist):
     for k, c in enumerate(inits):
         rt.upload(k, c)
     tile = rt.autotune(fold=2, reps=1)[:2]
+    strip_rows = rt.strip_rows()
     stream = torch.cuda.ExternalStream(rt.stream())
     for _ in range(args.warmup):
         rt.advance_async(FOLD)
@@ -440,6 +445,7 @@ def sweep_bench(args, torch, b2, ws, rank, dist):
         one = b2.Runtime([r], precision=prec)
         one.upload(0, c)
         one.set_tile(*tile)
+        one.set_strip_rows(strip_rows)
         one.advance(FOLD)
         s = torch.cuda.ExternalStream(one.stream())
         a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -463,7 +469,7 @@ def sweep_bench(args, torch, b2, ws, rank, dist):
             "data": "synthetic",
             "config": {"workload": "batched sweep: %d isothermal runs, sides 256-1024 in 64^2 blocks, fold 10"
                                    % args.sweep_runs, "runs_on_rank0": len(runs), "zones_rank0": zones,
-                       "tile": "%dx%d" % tuple(tile), "parallelism": "runs dealt to ranks" if dist else "single GPU"},
+                       "tile": "%dx%d" % tuple(tile), "strip_rows": strip_rows, "parallelism": "runs dealt to ranks" if dist else "single GPU"},
             "batched": {"value": value, "one_at_a_time": single_value, "ratio": value / single_value},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                          "frac": achieved / hbm_peak, "peak_kind": peak_kind, "traffic": None, "stage_ms": stage_ms},
@@ -472,16 +478,6 @@ def sweep_bench(args, torch, b2, ws, rank, dist):
     if dist:
         torch.distributed.destroy_process_group()
     return 0
-
-
-def make_tile_info(args, run, prec):
-    import binary2d as b2
-    rt = b2.Runtime([run], precision=prec)
-    if args.tile:
-        rt.set_tile(*[int(x) for x in args.tile.split("x")])
-    t = rt.tile()
-    rt.close()
-    return t
 
 
 def accuracy_check(prec, orbits):
@@ -522,7 +518,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="fp32_comp", choices=["fp64", "fp32_state64", "fp32_comp"])
     ap.add_argument("--workload", default="disk_2048")
-    ap.add_argument("--tile", default="")
+    ap.add_argument("--tile", default="", help="WxH: fixed tile instead of the autotuner")
+    ap.add_argument("--strip-rows", type=int, default=0,
+                    help="with --tile: row chunks across block rows for the paired FP32 kernel (0: off)")
     ap.add_argument("--sweep-runs", type=int, default=64)
     ap.add_argument("--tracers", type=int, default=-1, help="tracer particles (-1: workload default)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)

@@ -289,10 +289,24 @@ b2d_status b2d_initial_state(const b2d_config* cfg, const b2d_disk_model* model,
 b2d_status b2d_set_tile(b2d_ctx* ctx, int32_t tile_w, int32_t tile_h);
 b2d_status b2d_get_tile(const b2d_ctx* ctx, int32_t* tile_w, int32_t* tile_h);
 
+/* Row chunks of the paired-column FP32 stage kernel (precision FP32_COMP,
+ * isothermal, tile width 64 or 128).  rows > 0: every column strip of tile
+ * width is covered in ceil(N / rows) row chunks of near-equal height (at most
+ * `rows`; 8 <= rows <= block_size), each of which may cross one block
+ * boundary, so that the stage's CTAs can fill whole waves of the GPU; the
+ * tile height then applies only to the other stage kernels.  0 (default):
+ * block-aligned tiles of the tile height.  No reference counterpart: the
+ * reference advances block by block (src/scheme.rs:323-349); results and
+ * per-block ledgers do not depend on the tiling. */
+b2d_status b2d_set_strip_rows(b2d_ctx* ctx, int32_t rows);
+b2d_status b2d_get_strip_rows(const b2d_ctx* ctx, int32_t* rows);
+
 /* Tile autotuner: times every tile shape that divides the block size (width
- * 32..128, or 256 for FP64; height 8..128) over `reps` advances of `fold`
- * steps with CUDA events, keeps the fastest and reports it.  The context's
- * state is unchanged. */
+ * 32..128, or 256 for FP64; height 8..128) and, where the paired FP32 kernel
+ * runs, the strip rows that fill one, two or three whole waves of its
+ * resident CTAs, over `reps` advances of `fold` steps with CUDA events; keeps
+ * the fastest (b2d_get_tile and b2d_get_strip_rows report it).  The
+ * context's state is unchanged. */
 b2d_status b2d_autotune(b2d_ctx* ctx, int32_t fold, int32_t reps, int32_t* tile_w,
                         int32_t* tile_h, double* ms_per_stage);
 

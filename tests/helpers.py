@@ -24,13 +24,15 @@ def rel_err(a, b):
 
 
 def run_pair(mesh, hydro, physics, model, fold, advances, precision="fp64", tile=None, graphs=True,
-             background=None, nthreads=None):
+             background=None, nthreads=None, strip_rows=0):
     """Advance the same initial state on the GPU and on the oracle."""
     cons, cfg = make_case(mesh, hydro, physics, model)
     ref = binding.OracleState(cfg, cons, background=background)
     with b2.Runtime([b2.Run(mesh, hydro, physics)], precision=precision) as rt:
         if tile:
             rt.set_tile(*tile)
+        if strip_rows:
+            rt.set_strip_rows(strip_rows)
         rt.set_graphs(graphs)
         rt.upload(0, cons, background=background)
         dts, dts_ref = [], []

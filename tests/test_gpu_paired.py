@@ -90,3 +90,83 @@ def test_paired_kernel_batched_runs():
         for _ in range(3):
             ref.advance(5)
         assert rel_err(batched[k], ref.cons) <= TOL
+
+
+# Row chunks that cross block boundaries (b2d_set_strip_rows): mesh side N,
+# tile width, strip rows -> chunks of N / ceil(N / rows) rows
+CHUNKS = [
+    ((3, 64), 64, 40),     # 192 rows in 5 chunks of 38-39: crossings at rows 64 and 128
+    ((3, 64), 64, 20),     # 10 chunks of 19-20: block row 1 holds pieces of 4 chunks
+    ((2, 128), 128, 100),  # 3 chunks of 85-86, the middle one across row 128
+    ((2, 128), 64, 8),     # 32 chunks of 8 rows, block-aligned
+]
+
+
+@pytest.mark.parametrize("shape,tw,rows", CHUNKS)
+def test_paired_kernel_row_chunks(shape, tw, rows):
+    mesh, hydro, physics, model = b2.presets.iso_disk(*shape, seed=61)
+    r = run_pair(mesh, hydro, physics, model, fold=5, advances=3, precision="fp32_comp", tile=(tw, 32),
+                 strip_rows=rows)
+    check(r)
+
+
+def test_row_chunks_match_block_tiles():
+    """The zone updates do not depend on the tiling: the state (and so dt and
+    time) is bit-identical with block-aligned tiles and with chunks across
+    block rows; the per-block ledgers and orbital elements differ only by the
+    FP32 summation order of the tile pieces."""
+    mesh, hydro, physics, model = b2.presets.iso_disk(3, 64, seed=62)
+    cons = make_case(mesh, hydro, physics, model)[0]
+    out = {}
+    for rows in (0, 40, 20):
+        with b2.Runtime([b2.Run(mesh, hydro, physics)], precision="fp32_comp") as rt:
+            rt.set_tile(64, 32)
+            rt.set_strip_rows(rows)
+            assert rt.strip_rows() == rows
+            rt.upload(0, cons)
+            dts = [rt.advance(5)[0] for _ in range(3)]
+            s, t, it = rt.download(0)
+            out[rows] = (s, t, it, dts, rt.ledger(0), rt.elements(0))
+    s0, t0, it0, dts0, led0, el0 = out[0]
+    for rows in (40, 20):
+        s, t, it, dts, led, el = out[rows]
+        assert np.array_equal(s, s0)
+        assert t == t0 and it == it0 and dts == dts0
+        assert ledger_err(led, led0) <= 1e-5
+        escale = np.maximum(np.abs(el0).max(axis=(0, 1)), 1e-300)
+        assert (np.abs(el - el0).max(axis=(0, 1)) / escale).max() <= 1e-5
+
+
+def test_row_chunks_batched_runs():
+    """Runs of different sizes, each cut into its own row chunks, in one launch."""
+    cases = [b2.presets.iso_disk(nb, 64, seed=70 + k, q=q, e=e)
+             for k, (nb, q, e) in enumerate([(2, 1.0, 0.0), (3, 0.5, 0.3)])]
+    runs = [b2.Run(m, h, p) for m, h, p, _ in cases]
+    cons = [make_case(m, h, p, md)[0] for m, h, p, md in cases]
+    with b2.Runtime(runs, precision="fp32_comp") as rt:
+        rt.set_tile(64, 32)
+        rt.set_strip_rows(50)
+        for k, c in enumerate(cons):
+            rt.upload(k, c)
+        for _ in range(3):
+            rt.advance(5)
+        batched = [(rt.download(k)[0], rt.ledger(k)) for k in range(len(runs))]
+    for k, (m, h, p, md) in enumerate(cases):
+        ref = binding.OracleState(b2.to_c(m, h, p), cons[k])
+        for _ in range(3):
+            ref.advance(5)
+        assert rel_err(batched[k][0], ref.cons) <= TOL
+        items = [i for i in range(7) if i != BUFFER]
+        assert ledger_err(batched[k][1][:, :, items], ref.ledger[:, :, items]) <= LED_TOL
+
+
+def test_strip_rows_validation():
+    mesh, hydro, physics, model = b2.presets.iso_disk(2, 64, seed=63)
+    with b2.Runtime([b2.Run(mesh, hydro, physics)], precision="fp32_comp") as rt:
+        for bad in (-1, 4, 65):
+            with pytest.raises(Exception):
+                rt.set_strip_rows(bad)
+        rt.set_strip_rows(64)
+        assert rt.strip_rows() == 64
+        rt.set_strip_rows(0)
+        assert rt.strip_rows() == 0
