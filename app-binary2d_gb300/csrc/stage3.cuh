@@ -298,12 +298,16 @@ __global__ void __launch_bounds__(96, 4) stage3_kernel(StageArgs a)
     const int USLOT = s2_uslot_bytes(NF, 1, TW);
     unsigned char* slots = smem_raw;                          // stencil ring
     unsigned char* uslots = slots + S3_SLOTS * SLOT;          // update ring
-    float4* sP = (float4*)(uslots + S3_USLOTS * USLOT);       // [2][TW+4] primitives, column c at c+2
+    // float4 planes of two rows each.  Row slot c + 2 holds column c (face c for
+    // sF), the even slots in the first half of the row and the odd ones in the
+    // second: a pair's two records sit in the two halves, so a warp's accesses
+    // are 16 bytes apart (no bank conflicts; adjacent float4s would be 2-way).
+    float4* sP = (float4*)(uslots + S3_USLOTS * USLOT);       // [2][TW+4] primitives
     // cell records, column c at c+2: R0 = pc, gy0 | R1 = gy1, gy2, tyy, txy | R2 = gx, txx
     float4* sR0 = sP + 2 * (TW + 4);                          // [2][TW+4]
     float4* sR1 = sR0 + 2 * (TW + 4);
     float4* sR2 = sR1 + 2 * (TW + 4);
-    float4* sF = sR2 + 2 * (TW + 4);                          // [2][TW+2] y-face fluxes, face c at c
+    float4* sF = sR2 + 2 * (TW + 4);                          // [2][TW+2] y-face fluxes
     uint64_t* bars = (uint64_t*)(sF + 2 * (TW + 2));          // [S3_SLOTS] stencil ring
     uint64_t* ubars = bars + S3_SLOTS;                        // [S3_USLOTS] update ring
 
@@ -313,6 +317,8 @@ __global__ void __launch_bounds__(96, 4) stage3_kernel(StageArgs a)
     const bool active = interior || (hl >= 0 && hl < 2);
     const int c0 = interior ? 2 * t : (hl == 0 ? -2 : TW);   // first column of this thread's pair
     const bool producer = (hl == 4);
+    const int p = c0 >> 1;                                   // the pair's slot in a half row (-1 for the -2 pair)
+    const int HR = TW / 2 + 2, HF = TW / 2 + 1;              // odd halves of the record and flux rows
 
     auto plane = [&](const float* base, int f, int part) -> const float* { return base + (size_t)(2 * f + part) * nn; };
     auto copy_row = [&](unsigned char* dst, const float* row, int w_halo, uint64_t* bar) {
@@ -428,17 +434,17 @@ __global__ void __launch_bounds__(96, 4) stage3_kernel(StageArgs a)
             }
 #pragma unroll
             for (int f = 0; f < NF; ++f) pn[f] = make_float2(pa[f], pb[f]);
-            float4* row = sP + (rn & 1) * (TW + 4) + c0 + 2;
+            float4* row = sP + (rn & 1) * (TW + 4) + p + 1;
             row[0] = make_float4(pa[0], pa[1], pa[2], 0.0f);
-            row[1] = make_float4(pb[0], pb[1], pb[2], 0.0f);
+            row[HR] = make_float4(pb[0], pb[1], pb[2], 0.0f);
         }
 
         // ---- phase 2: slopes and cell records of row rg = rn - 1 (scheme.rs:216-254) ---
         const int rg = rn - 1;
         if (rg >= -1 && rg <= TH && active) {
             const float4* prow = sP + (rg & 1) * (TW + 4);
-            const float4 l4 = prow[max(c0 + 1, 0)];            // column c0 - 1 (clamped for the -2 pair)
-            const float4 r4 = prow[min(c0 + 4, TW + 3)];       // column c0 + 2 (clamped for the TW pair)
+            const float4 l4 = prow[HR + p];                    // column c0 - 1 (in the row, unused, for the -2 pair)
+            const float4 r4 = prow[p + 2];                     // column c0 + 2 (in the row, unused, for the TW pair)
             const float lv[3] = {l4.x, l4.y, l4.z}, rv[3] = {r4.x, r4.y, r4.z};
             const float2 thx = make_float2((Pm1[0].x < pdt || P0[0].x < pdt || pn[0].x < pdt) ? 0.0f : theta,
                                            (Pm1[0].y < pdt || P0[0].y < pdt || pn[0].y < pdt) ? 0.0f : theta);
@@ -458,13 +464,13 @@ __global__ void __launch_bounds__(96, 4) stage3_kernel(StageArgs a)
             const float2 tyy = mul2(cv, fma2(f2(4.0f / 3.0f), db, fma2(f2(-2.0f / 3.0f), da, lb)));
             const float2 txy = mul2(cv, mul2(add2(gx[2], gy[1]), f2(inv_dx)));
             // cell records of both columns
-            const int o = (rg & 1) * (TW + 4) + c0 + 2;
+            const int o = (rg & 1) * (TW + 4) + p + 1;
             sR0[o] = make_float4(P0[0].x, P0[1].x, P0[2].x, gy[0].x);
             sR1[o] = make_float4(gy[1].x, gy[2].x, tyy.x, txy.x);
             sR2[o] = make_float4(gx[0].x, gx[1].x, gx[2].x, txx.x);
-            sR0[o + 1] = make_float4(P0[0].y, P0[1].y, P0[2].y, gy[0].y);
-            sR1[o + 1] = make_float4(gy[1].y, gy[2].y, tyy.y, txy.y);
-            sR2[o + 1] = make_float4(gx[0].y, gx[1].y, gx[2].y, txx.y);
+            sR0[o + HR] = make_float4(P0[0].y, P0[1].y, P0[2].y, gy[0].y);
+            sR1[o + HR] = make_float4(gy[1].y, gy[2].y, tyy.y, txy.y);
+            sR2[o + HR] = make_float4(gx[0].y, gx[1].y, gx[2].y, txx.y);
 #pragma unroll
             for (int f = 0; f < NF; ++f) xg[f] = gx[f];
             xtn = txx;
@@ -483,10 +489,10 @@ __global__ void __launch_bounds__(96, 4) stage3_kernel(StageArgs a)
         const bool up_ok = ru >= 0 && ru <= TH - 1;
         // y fluxes of row rq at faces c0 and c0 + 1 (cells c0-1 | c0 and c0 | c0+1)
         auto y_flux = [&]() {
-            const int ob = (rq & 1) * (TW + 4) + c0 + 1;      // record of column c0 - 1
-            const float4 a0 = sR0[ob], a1 = sR1[ob];
+            const int ob = (rq & 1) * (TW + 4) + p;           // records of columns c0 - 1, c0, c0 + 1
+            const float4 a0 = sR0[ob + HR], a1 = sR1[ob + HR];
             const float4 b0 = sR0[ob + 1], b1 = sR1[ob + 1];
-            const float4 d0 = sR0[ob + 2], d1 = sR1[ob + 2];
+            const float4 d0 = sR0[ob + HR + 1], d1 = sR1[ob + HR + 1];
             const float2 pcl[3] = {make_float2(a0.x, b0.x), make_float2(a0.y, b0.y), make_float2(a0.z, b0.z)};
             const float2 gl[3] = {make_float2(a0.w, b0.w), make_float2(a1.x, b1.x), make_float2(a1.y, b1.y)};
             const float2 pcr[3] = {make_float2(b0.x, d0.x), make_float2(b0.y, d0.y), make_float2(b0.z, d0.z)};
@@ -498,9 +504,9 @@ __global__ void __launch_bounds__(96, 4) stage3_kernel(StageArgs a)
             face_flux2<1>(P, B, pcl, gl, make_float2(a1.z, b1.z), make_float2(a1.w, b1.w), pcr, gr,
                           make_float2(b1.z, d1.z), make_float2(b1.w, d1.w), f2(x), yv2, cs2, F);
             if (fy_ok) {
-                float4* fo = sF + (rq & 1) * (TW + 2) + c0;
+                float4* fo = sF + (rq & 1) * (TW + 2) + p;
                 fo[0] = make_float4(F[0].x, F[1].x, F[2].x, 0.0f);
-                fo[1] = make_float4(F[0].y, F[1].y, F[2].y, 0.0f);
+                fo[HF] = make_float4(F[0].y, F[1].y, F[2].y, 0.0f);
             }
         };
         float2 fxn[NF];
@@ -513,8 +519,8 @@ __global__ void __launch_bounds__(96, 4) stage3_kernel(StageArgs a)
             {
                 const int rc = min(max(ru, 0), TH - 1);
                 const float* sb = (const float*)(slots + ((rc + 2) % S3_SLOTS) * SLOT);
-                const float4* frow = sF + (ru & 1) * (TW + 2) + c0;
-                const float4 fa = frow[0], fb = frow[1], fc = frow[2];
+                const float4* frow = sF + (ru & 1) * (TW + 2) + p;   // faces c0, c0 + 1, c0 + 2
+                const float4 fa = frow[0], fb = frow[HF], fc = frow[1];
                 const float2 fyl[3] = {make_float2(fa.x, fb.x), make_float2(fa.y, fb.y), make_float2(fa.z, fb.z)};
                 const float2 fyr[3] = {make_float2(fb.x, fc.x), make_float2(fb.y, fc.y), make_float2(fb.z, fc.z)};
                 const float x = xc_row[rc];
@@ -665,8 +671,9 @@ __global__ void __launch_bounds__(96, 4) stage3_kernel(StageArgs a)
             // memory, row rq + 1 = rg's from this iteration's registers (primitives
             // in Pm1 after the rotation)
             {
-                const int oa = (rq & 1) * (TW + 4) + c0 + 2;
-                const float4 a0 = sR0[oa], a1 = sR1[oa], a2 = sR2[oa], e0 = sR0[oa + 1], e1 = sR1[oa + 1], e2 = sR2[oa + 1];
+                const int oa = (rq & 1) * (TW + 4) + p + 1;
+                const float4 a0 = sR0[oa], a1 = sR1[oa], a2 = sR2[oa];
+                const float4 e0 = sR0[oa + HR], e1 = sR1[oa + HR], e2 = sR2[oa + HR];
                 const float2 pcl[3] = {make_float2(a0.x, e0.x), make_float2(a0.y, e0.y), make_float2(a0.z, e0.z)};
                 const float2 gl[3] = {make_float2(a2.x, e2.x), make_float2(a2.y, e2.y), make_float2(a2.z, e2.z)};
                 const float x = xv_row[min(max(rq + 1, 0), TH)];
