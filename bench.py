@@ -49,19 +49,50 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def ncu_traffic(workload, precision):
-    """DRAM bytes (read + write) of one stage-kernel launch from the committed
-    ncu summary of this workload, or None."""
-    name = {("disk_2048", "fp32_comp"): "stage3_kernel_fp32comp_disk2048.md"}.get((workload, precision))
+def link_bandwidth(torch, host_src, host_dst):
+    """Host-to-device and device-to-host copy rates (GB/s) of one page-locked
+    state-sized buffer, measured with CUDA events: what bounds the end-to-end
+    leg when a step's copies outlast its advance."""
+    dev = torch.empty(host_src.nbytes, dtype=torch.uint8, device="cuda")
+    src = torch.from_numpy(host_src.view(np.uint8).reshape(-1))
+    dst = torch.from_numpy(host_dst.view(np.uint8).reshape(-1))
+    e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    dev.copy_(src, non_blocking=True)
+    dst.copy_(dev, non_blocking=True)
+    e0.record()
+    dev.copy_(src, non_blocking=True)
+    e1.record()
+    dst.copy_(dev, non_blocking=True)
+    e2.record()
+    e2.synchronize()
+    n = host_src.nbytes / 1e6
+    out = {"h2d": n / e0.elapsed_time(e1), "d2h": n / e1.elapsed_time(e2)}
+    del dev
+    return out
+
+
+PROFILES = {("disk_2048", "fp32_comp"): "stage3_kernel_fp32comp_disk2048.md"}
+
+
+def ncu_profile(workload, precision, key):
+    """A row (`| key | value |`) of the committed ncu summary of this workload's
+    stage kernel, or None."""
+    name = PROFILES.get((workload, precision))
     if not name:
         return None
     try:
         for line in open(os.path.join(ROOT, "profiles", name)):
-            if line.startswith("| traffic_bytes_per_launch |"):
-                return int(line.split("|")[2])
-    except (OSError, ValueError):
+            if line.startswith("| %s |" % key):
+                return line.split("|")[2].strip()
+    except OSError:
         return None
     return None
+
+
+def ncu_traffic(workload, precision):
+    """DRAM bytes (read + write) of one stage-kernel launch, or None."""
+    v = ncu_profile(workload, precision, "traffic_bytes_per_launch")
+    return int(v) if v else None
 
 
 def dist_env():
@@ -297,6 +328,7 @@ def ours(args):
     host_out = [np.empty_like(cons) for _ in range(2)]
     for a in host_in + host_out:
         b2.pin(a)
+    copy_gbs = link_bandwidth(torch, host_in[0], host_out[0])
     rt = make(prec)
 
     def e2e_step(k):
@@ -368,18 +400,17 @@ def ours(args):
                          "frac": achieved / hbm_peak, "peak_kind": peak_kind,
                          "traffic": ncu_traffic(args.workload, prec),
                          "traffic_note": ("mean DRAM bytes of the two RK2 stage launches of one step "
-                                          "(algorithmic mean 352 MB) from profiles/stage3_kernel_fp32comp_disk2048.md")
+                                          "(algorithmic mean 352 MB) from profiles/" + PROFILES[(args.workload, prec)])
                                          if ncu_traffic(args.workload, prec) else "no ncu capture of this workload",
                          "algorithmic_bytes_per_launch": bytes_per_launch,
                          "bytes_per_zone_update": bytes_per_zone_update, "stage_ms": stage_ms,
-                         "limiter": ("instruction issue and latency at 12 warps/SM (ncu: 52% issue active, "
-                                     "676 warp instructions per zone-stage, DRAM 17-25% of peak)")
-                                    if ncu_traffic(args.workload, prec) else "instruction issue (no ncu capture of this workload)"},
+                         "limiter": ncu_profile(args.workload, prec, "limiter")
+                                    or "instruction issue (no ncu capture of this workload)"},
             "fp64": {"value": fp64_value, "ratio": (value / fp64_value) if fp64_value else None},
             "accuracy": accuracy,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(cons.nbytes),
-                    "d2h_bytes_per_step": int(cons.nbytes)},
+                    "d2h_bytes_per_step": int(cons.nbytes), "link_gbs": copy_gbs},
             "gpu_launches": int(launches),
             "clocks": clk.summary(),
         }
