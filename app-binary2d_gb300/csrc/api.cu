@@ -390,8 +390,13 @@ static int default_tile_w(int bs)
 static bool tile_ok(const b2d_ctx* ctx, int tw, int th)
 {
     if (tw < 1 || th < 1 || tw > 256) return false;
-    for (const RunHost& r : ctx->runs)
-        if (r.bs % tw || r.bs % th) return false;
+    // the paired FP32 kernel's 128- and 256-column tiles may also span whole
+    // blocks side by side (blocks of 64 columns or more)
+    const bool span = ctx->precision == B2D_PREC_FP32_COMP && ctx->nf == 3 && (tw == 128 || tw == 256);
+    for (const RunHost& r : ctx->runs) {
+        if (r.bs % th) return false;
+        if (r.bs % tw && !(span && r.bs >= 64 && tw % r.bs == 0 && r.N % tw == 0)) return false;
+    }
     if (tw % 32 != 0) {
         // a partial warp is allowed only when it is the whole block width
         for (const RunHost& r : ctx->runs)
@@ -434,7 +439,7 @@ static void free_ctx(b2d_ctx* ctx)
 // (launch_stage_f32 makes the same choice).
 static bool paired_kernel(const b2d_ctx* ctx)
 {
-    return ctx->precision == B2D_PREC_FP32_COMP && ctx->nf == 3 && ctx->tw % 64 == 0 && ctx->tw <= 128;
+    return ctx->precision == B2D_PREC_FP32_COMP && ctx->nf == 3 && (ctx->tw == 64 || ctx->tw == 128 || ctx->tw == 256);
 }
 
 // Row chunks per column strip of a run: block-aligned tiles of height th, or,
@@ -460,7 +465,7 @@ static b2d_status sync_rundev(b2d_ctx* ctx)
         // bs / th for block-aligned tiles)
         int most = 0;
         for (int b = 0; b < r.nb; ++b) most = std::max(most, chunks_in_block_row(b, r.bs, r.N, d.tiles_i));
-        d.tiles_per_block = most * (r.bs / ctx->tw);
+        d.tiles_per_block = most * std::max(r.bs / ctx->tw, 1);
         base += d.ntiles;
         CUDA_TRY(cudaFree(r.partial));
         r.partial = nullptr;
@@ -1593,7 +1598,7 @@ extern "C" b2d_status b2d_autotune(b2d_ctx* ctx, int32_t fold, int32_t reps, int
     b2d_status st = ensure_stage_capacity(ctx, fold);
     if (st != B2D_OK) return st;
     CUDA_TRY(cudaStreamSynchronize(ctx->stream));
-    const int max_w = ctx->precision == B2D_PREC_FP64 ? 256 : 128;
+    const int max_w = ctx->precision == B2D_PREC_FP64 || (ctx->precision == B2D_PREC_FP32_COMP && ctx->nf == 3) ? 256 : 128;
     int best_w = ctx->tw, best_h = ctx->th, best_rows = 0;
     double best = 1e300;
     ctx->strip_rows = 0;
@@ -1611,8 +1616,8 @@ extern "C" b2d_status b2d_autotune(b2d_ctx* ctx, int32_t fold, int32_t reps, int
             if (ms < best) { best = ms; best_w = w; best_h = h; }
         }
     }
-    // row chunks of the paired kernel, at both of its tile widths
-    for (int w : {64, 128}) {
+    // row chunks of the paired kernel, at each of its tile widths
+    for (int w : {64, 128, 256}) {
         int h = 0;
         for (int hh : {64, 32, 16, 8})
             if (!h && tile_ok(ctx, w, hh)) h = hh;

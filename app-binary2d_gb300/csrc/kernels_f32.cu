@@ -33,10 +33,10 @@ static cudaError_t launch_two(const StageArgs& a, int grid, int tw, cudaStream_t
     return launch_two_impl<NF, STORE, false>(a, grid, tw, s);
 }
 
-template <bool SINGLE>
+template <bool SINGLE, bool WIDE>
 static cudaError_t launch_three_impl(const StageArgs& a, int grid, int tw, cudaStream_t s)
 {
-    auto k = stage3_kernel<SINGLE>;
+    auto k = stage3_kernel<SINGLE, WIDE>;
     size_t smem = s3_smem_bytes(tw);
     static size_t configured = 0;
     if (smem > configured) {
@@ -54,16 +54,23 @@ int paired_ctas_per_sm(int nruns, int tw)
 {
     const size_t smem = s3_smem_bytes(tw);
     int n = 0;
+    const bool wide = tw == 256;
     cudaError_t e = nruns == 1
-        ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, stage3_kernel<true>, tw / 2 + 32, smem)
-        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, stage3_kernel<false>, tw / 2 + 32, smem);
+        ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+              &n, wide ? stage3_kernel<true, true> : stage3_kernel<true, false>, tw / 2 + 32, smem)
+        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+              &n, wide ? stage3_kernel<false, true> : stage3_kernel<false, false>, tw / 2 + 32, smem);
     return e == cudaSuccess ? n : 0;
 }
 
 cudaError_t launch_stage_f32(int nf, int store, const StageArgs& a, int grid, int tw, size_t smem, cudaStream_t s)
 {
-    if (nf == 3 && store == 1 && tw % 64 == 0 && tw <= 128)
-        return a.nruns == 1 ? launch_three_impl<true>(a, grid, tw, s) : launch_three_impl<false>(a, grid, tw, s);
+    if (nf == 3 && store == 1 && (tw == 64 || tw == 128))
+        return a.nruns == 1 ? launch_three_impl<true, false>(a, grid, tw, s)
+                            : launch_three_impl<false, false>(a, grid, tw, s);
+    if (nf == 3 && store == 1 && tw == 256)
+        return a.nruns == 1 ? launch_three_impl<true, true>(a, grid, tw, s)
+                            : launch_three_impl<false, true>(a, grid, tw, s);
     if (tw % 32 == 0 && tw <= 128) {
         if (nf == 3) return store == 0 ? launch_two<3, 0>(a, grid, tw, s) : launch_two<3, 1>(a, grid, tw, s);
         return store == 0 ? launch_two<4, 0>(a, grid, tw, s) : launch_two<4, 1>(a, grid, tw, s);

@@ -160,6 +160,7 @@ __device__ __forceinline__ void face_flux2(const DevParamsF& P, const Binary<flo
 constexpr int S3_DEPTH = 1;
 constexpr int S3_SLOTS = S3_DEPTH + 4;   // stencil ring: a row is read again 3 rows after it lands
 constexpr int S3_USLOTS = S3_DEPTH + 1;  // update ring
+constexpr int S3_MAX_TP = 128;           // interior threads of the widest tile (256 columns)
 
 __host__ __device__ inline int s3_smem_bytes(int tw)
 {
@@ -168,31 +169,35 @@ __host__ __device__ inline int s3_smem_bytes(int tw)
     return slots + exch + 8 * (S3_SLOTS + S3_USLOTS);
 }
 
-// One ledger piece of a tile (its rows in block row brow), by one warp after
-// the row loop: sums over the interior warps' bank rows, the piece's slot in
-// the block's partials, and the fold of the block's pieces (in piece order)
-// by the block's last piece.  acc (a crossing tile's first piece) holds group
-// 0 per thread, to be reduced here first.  Out of line, so that it does not
-// weigh on the row loop's register allocation; no CTA barrier, so that two
-// warps can flush two pieces at once.
+// One ledger piece of a tile (its columns in block (brow, bj)), by one warp
+// after the row loop: sums over the bank rows of the nw interior warps over
+// those columns, the piece's slot in the block's partials, and the fold of
+// the block's pieces (in piece order) by the block's last piece.  acc (a
+// crossing tile's first piece) holds group 0 per thread of those warps, to be
+// reduced here first.  Out of line, so that it does not weigh on the row
+// loop's register allocation; no CTA barrier, so that warps can flush
+// several pieces at once.
 template <int NF>
 __device__ __noinline__ void flush_piece(const RunDev& rd, int brow, int bj, int lslot, int TW, float (*bank)[32],
-                                         const float (*acc)[64], int in_slot, int base_slot, int out_slot,
-                                         int stage, double bf)
+                                         int nw, const float (*acc)[S3_MAX_TP], int in_slot, int base_slot,
+                                         int out_slot, int stage, double bf)
 {
     constexpr int NL = NITEMS * NF;
-    const int lane = threadIdx.x & 31, TP = TW / 2;
+    const int lane = threadIdx.x & 31;
     if (acc) {
         float v0[8];
 #pragma unroll
-        for (int m = 0; m < 7; ++m) v0[m] = acc[m][lane] + (TP > 32 ? acc[m][lane + 32] : 0.0f);
+        for (int m = 0; m < 7; ++m) {
+            v0[m] = 0.0f;
+            for (int w = 0; w < nw; ++w) v0[m] += acc[m][lane + 32 * w];
+        }
         v0[7] = 0.0f;
         const float s0 = warp_sum_items<8>(v0, lane);
         const int slot0 = group_writer_slot<NF, 0>(lane);
         if (slot0 >= 0) bank[0][slot0] += s0;
         __syncwarp();
     }
-    const int bs = rd.bs, nc = rd.tiles_i, per_row = bs / TW;
+    const int bs = rd.bs, nc = rd.tiles_i, per_row = max(bs / TW, 1);
     const int ti = ((int)blockIdx.x - rd.tile_base) / rd.tiles_j;
     const int block = brow * rd.nb + bj;
     const int piece = (ti - chunk_of_row(brow * bs, rd.N, nc)) * per_row + lslot;
@@ -206,7 +211,7 @@ __device__ __noinline__ void flush_piece(const RunDev& rd, int brow, int bj, int
         }
         double s = 0.0;
         if (live)
-            for (int w = 0; w < TP / 32; ++w) s += (double)bank[w][j];
+            for (int w = 0; w < nw; ++w) s += (double)bank[w][j];
         rd.partial[((size_t)block * rd.tiles_per_block + piece) * NL + lane] = s;
         __threadfence();   // visible before the counter below counts this piece
     }
@@ -230,8 +235,11 @@ __device__ __noinline__ void flush_piece(const RunDev& rd, int brow, int bj, int
     if (lane == 0) rd.counter[block] = 0u;
 }
 
-template <bool SINGLE>
-__global__ void __launch_bounds__(96, 4) stage3_kernel(StageArgs a)
+// WIDE: 256-column tiles over two 128-column blocks (or one 256-column block),
+// 4 interior warps to each halo warp, 2 CTAs per SM; otherwise 64- or
+// 128-column tiles, 4 CTAs per SM.
+template <bool SINGLE, bool WIDE>
+__global__ void __launch_bounds__(WIDE ? 160 : 96, WIDE ? 2 : 4) stage3_kernel(StageArgs a)
 {
     constexpr int NF = 3;
     constexpr int H = 4;                     // staged halo columns per side: 16 bytes of FP32
@@ -280,7 +288,7 @@ __global__ void __launch_bounds__(96, 4) stage3_kernel(StageArgs a)
     const int rb = min(bs - i0 % bs, TH);
     const int bl = (i0 + TH - 1) / bs;
     const int block = bl * rd.nb + bj;
-    const int tib = (ti - chunk_of_row(bl * bs, N, C)) * (bs / TW) + lj0 / TW;
+    const int tib = (ti - chunk_of_row(bl * bs, N, C)) * max(bs / TW, 1) + lj0 / TW;
     const bool has_base = a.base_slot >= 0;
 
     const float* uin = (const float*)rd.slot[a.in_slot];
@@ -290,7 +298,6 @@ __global__ void __launch_bounds__(96, 4) stage3_kernel(StageArgs a)
     const float dt = (float)*rd.dt;
     const float time = (float)rd.stage_time[a.stage];
     const float* xc = rd.xcf;
-    const float* xv = rd.xvf;
 
     // ---- shared memory carve-up ------------------------------------------------
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -371,8 +378,7 @@ __global__ void __launch_bounds__(96, 4) stage3_kernel(StageArgs a)
     const bool want_amax = a.amax_flag != 0;
     // positions: zone centres (y) of the pair, y of the pair's left faces
     const float2 yc2 = interior ? make_float2(xc[j0 + c0], xc[j0 + c0 + 1]) : f2(0.0f);
-    const int fv = bj * (bs + 1) + lj0;
-    const float2 yv2 = (interior || hl == 1) ? make_float2(xv[fv + c0], xv[fv + min(c0 + 1, TW)]) : f2(0.0f);
+    const float2 yv2 = (interior || hl == 1) ? make_float2(rd.xvgf[j0 + c0], rd.xvgf[j0 + min(c0 + 1, TW)]) : f2(0.0f);
     const float* xv_row = rd.xvgf + i0;
     const float* xc_row = xc + i0;
     // dy^2 + s^2 of a pair of y positions to each body (recomputed where used:
@@ -389,7 +395,7 @@ __global__ void __launch_bounds__(96, 4) stage3_kernel(StageArgs a)
     static_assert(group_size<NF, 0>() + group_size<NF, 1>() + group_size<NF, 2>() == NLIVE, "ledger groups");
     // [warp][item slot] of the main piece and of a crossing tile's first piece;
     // group 0 of the first piece per thread
-    __shared__ float sLed[4][32], sLedA[4][32], sAccA[7][64];
+    __shared__ float sLed[4][32], sLedA[4][32], sAccA[7][S3_MAX_TP];
     const int lane = t & 31, warp = t >> 5;
     if (t < 128) sLed[t >> 5][t & 31] = sLedA[t >> 5][t & 31] = 0.0f;
     const int slot0 = group_writer_slot<NF, 0>(lane);
@@ -705,8 +711,8 @@ __global__ void __launch_bounds__(96, 4) stage3_kernel(StageArgs a)
     }
     if (t == 0 && timeout) atomicOr(a.timeout_flag, 1u);
 
-    // ---- ledger pieces: the main piece by warp 0 and a crossing tile's first piece
-    // (the block row above) by the halo warp, at once ------------------------------
+    // ---- ledger pieces, one per block under the tile: its block row(s) times its
+    // block column(s), each flushed by its own warp --------------------------------
     if (interior) {   // whole warps: group 0's column sums, one warp reduction per tile
         float v0[8];
 #pragma unroll
@@ -716,13 +722,20 @@ __global__ void __launch_bounds__(96, 4) stage3_kernel(StageArgs a)
         if (slot0 >= 0) sLed[warp][slot0] += s0;
     }
     __syncthreads();
-    const int brow = block / rd.nb, lslot = tib % (rd.bs / TW);
-    if (warp == 0)
-        flush_piece<NF>(rd, brow, block - brow * rd.nb, lslot, TW, sLed, nullptr, a.in_slot, a.base_slot, a.out_slot,
-                        a.stage, a.bf);
-    else if (warp == TP / 32 && rb < TH)
-        flush_piece<NF>(rd, brow - 1, block - brow * rd.nb, lslot, TW, sLedA, sAccA, a.in_slot, a.base_slot,
-                        a.out_slot, a.stage, a.bf);
+    const int brow = block / rd.nb, bcol = block - brow * rd.nb;
+    const int ncol = max(TW / rd.bs, 1), wpc = TP / 32 / ncol;   // block columns; interior warps over each
+    const int lslot = tib % max(rd.bs / TW, 1);
+    const int npiece = (rb < TH ? 2 : 1) * ncol;                 // the main block row's pieces, then the first's
+    for (int k = warp; k < npiece; k += blockDim.x / 32) {
+        const int c = k % ncol;
+        if (k < ncol)
+            flush_piece<NF>(rd, brow, bcol + c, lslot, TW, sLed + c * wpc, wpc, nullptr, a.in_slot, a.base_slot,
+                            a.out_slot, a.stage, a.bf);
+        else
+            flush_piece<NF>(rd, brow - 1, bcol + c, lslot, TW, sLedA + c * wpc, wpc,
+                            (const float (*)[S3_MAX_TP])(&sAccA[0][c * wpc * 32]), a.in_slot, a.base_slot,
+                            a.out_slot, a.stage, a.bf);
+    }
 }
 
 }  // namespace b2d

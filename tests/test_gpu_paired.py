@@ -1,6 +1,7 @@
-"""The paired-column FP32 kernel (isothermal, compensated FP32 state, tiles a
-multiple of 64 wide) against the CPU oracle: every isothermal physics
-variant, both tile widths, single and batched launches."""
+"""The paired-column FP32 kernel (isothermal, compensated FP32 state, tiles 64,
+128 or 256 wide) against the CPU oracle: every isothermal physics variant,
+every tile width, row chunks across block rows and tiles across block
+columns, single and batched launches."""
 import dataclasses
 
 import numpy as np
@@ -99,6 +100,10 @@ CHUNKS = [
     ((3, 64), 64, 20),     # 10 chunks of 19-20: block row 1 holds pieces of 4 chunks
     ((2, 128), 128, 100),  # 3 chunks of 85-86, the middle one across row 128
     ((2, 128), 64, 8),     # 32 chunks of 8 rows, block-aligned
+    ((2, 128), 256, 100),  # 256-column tiles over both block columns, 3 chunks
+    ((2, 128), 256, 0),    # 256-column tiles, block-aligned rows (256 x 32)
+    ((4, 64), 128, 50),    # 128-column tiles over two 64-column blocks, 6 chunks
+    ((4, 64), 128, 0),
 ]
 
 
@@ -132,6 +137,33 @@ def test_row_chunks_match_block_tiles():
         s, t, it, dts, led, el = out[rows]
         assert np.array_equal(s, s0)
         assert t == t0 and it == it0 and dts == dts0
+        assert ledger_err(led, led0) <= 1e-5
+        escale = np.maximum(np.abs(el0).max(axis=(0, 1)), 1e-300)
+        assert (np.abs(el - el0).max(axis=(0, 1)) / escale).max() <= 1e-5
+
+
+@pytest.mark.parametrize("nb,bs,tiles", [(4, 64, [(64, 32, 0), (128, 32, 0), (128, 32, 50), (64, 16, 30)]),
+                                          (2, 128, [(128, 32, 0), (256, 32, 0), (256, 32, 100), (256, 64, 40)])])
+def test_tiles_spanning_blocks_match(nb, bs, tiles):
+    """Tiles over two block columns (and row chunks over block rows) give the
+    state of block-aligned tiles bit for bit, and its ledgers to FP32
+    summation order."""
+    mesh, hydro, physics, model = b2.presets.iso_disk(nb, bs, seed=64)
+    cons = make_case(mesh, hydro, physics, model)[0]
+    out = []
+    for tw, th, rows in tiles:
+        with b2.Runtime([b2.Run(mesh, hydro, physics)], precision="fp32_comp") as rt:
+            rt.set_tile(tw, th)
+            rt.set_strip_rows(rows)
+            assert rt.tile() == (tw, th)
+            rt.upload(0, cons)
+            dts = [rt.advance(5)[0] for _ in range(3)]
+            s, t, it = rt.download(0)
+            out.append((s, t, dts, rt.ledger(0), rt.elements(0)))
+    s0, t0, dts0, led0, el0 = out[0]
+    for s, t, dts, led, el in out[1:]:
+        assert np.array_equal(s, s0)
+        assert t == t0 and dts == dts0
         assert ledger_err(led, led0) <= 1e-5
         escale = np.maximum(np.abs(el0).max(axis=(0, 1)), 1e-300)
         assert (np.abs(el - el0).max(axis=(0, 1)) / escale).max() <= 1e-5
