@@ -285,12 +285,14 @@ b2d_status b2d_initial_state(const b2d_config* cfg, const b2d_disk_model* model,
 
 /* Tile shape of the stage kernel for a context: width in zones along j (a
  * multiple of 32 dividing block_size) and height along i (dividing
- * block_size).  0 keeps the current value. */
+ * block_size).  The paired-column FP32 kernel (precision FP32_COMP,
+ * isothermal) also takes 128- or 256-column tiles that span whole blocks of
+ * 64 columns or more side by side.  0 keeps the current value. */
 b2d_status b2d_set_tile(b2d_ctx* ctx, int32_t tile_w, int32_t tile_h);
 b2d_status b2d_get_tile(const b2d_ctx* ctx, int32_t* tile_w, int32_t* tile_h);
 
 /* Row chunks of the paired-column FP32 stage kernel (precision FP32_COMP,
- * isothermal, tile width 64 or 128).  rows > 0: every column strip of tile
+ * isothermal, tile width 64, 128 or 256).  rows > 0: every column strip of tile
  * width is covered in ceil(N / rows) row chunks of near-equal height (at most
  * `rows`; 8 <= rows <= block_size), each of which may cross one block
  * boundary, so that the stage's CTAs can fill whole waves of the GPU; the
