@@ -161,59 +161,82 @@ __global__ void max_speed_kernel(const RunDev* runs, int run, int slot)
 }
 
 // Block layout [nb][nb][bs][bs][nf] (host) <-> field planes (device).  A CTA
-// row handles one row of one mesh block (grid: nb^2 x bs), its threads the
-// row's bs * nf consecutive host-side elements, so the host side (which may
-// be a page-locked host buffer read or written in place over the CPU-GPU
-// link) is a contiguous, coalesced sweep and the index arithmetic is one
-// division by nf per element.
-__device__ __forceinline__ void row_origin(int N, int bs, int nb, int nf, size_t& e0, size_t& z0)
+// takes LAYOUT_ZONES consecutive zones of the host layout: the host side
+// (which may be a page-locked host buffer read or written in place over the
+// CPU-GPU link) moves as one contiguous, coalesced sweep through shared
+// memory, and each field plane is written (read) by one thread per zone, 32
+// consecutive words per warp.
+constexpr int LAYOUT_ZONES = 256;
+
+// Plane index of host-layout zone q (block-major: block, row, column).
+__device__ __forceinline__ size_t plane_index(size_t q, int N, int bs, int nb)
 {
-    const int blk = blockIdx.x, li = blockIdx.y;
-    const int bi = blk / nb, bj = blk - bi * nb;
-    e0 = ((size_t)blk * bs + li) * (size_t)bs * nf;
-    z0 = (size_t)(bi * bs + li) * N + (size_t)bj * bs;
+    const size_t r = q / bs;
+    const int lj = (int)(q - r * bs);
+    const size_t b = r / bs;
+    const int li = (int)(r - b * bs);
+    const int bi = (int)(b / nb), bj = (int)(b - (size_t)bi * nb);
+    return (size_t)(bi * bs + li) * N + (size_t)bj * bs + lj;
 }
 
-__device__ __forceinline__ int zone_of(int t, int nf) { return nf == 3 ? t / 3 : t >> 2; }
-
-__global__ void scatter_kernel(const double* src, void* dst, int N, int bs, int nb, int nf, int store)
+__global__ void __launch_bounds__(LAYOUT_ZONES) scatter_kernel(const double* src, void* dst, int N, int bs, int nb,
+                                                               int nf, int store)
 {
+    __shared__ double buf[LAYOUT_ZONES * 4];
     const size_t nn = (size_t)N * N;
-    size_t e0, z0;
-    row_origin(N, bs, nb, nf, e0, z0);
-    for (int t = threadIdx.x; t < bs * nf; t += blockDim.x) {
-        const int lj = zone_of(t, nf), f = t - lj * nf;
-        const double v = src[e0 + t];
-        const size_t z = z0 + lj;
-        if (store == 0) {
-            ((double*)dst)[f * nn + z] = v;
-        } else {
-            const float hi = (float)v;
-            const float lo = (float)(v - (double)hi);
-            ((float*)dst)[(2 * f) * nn + z] = hi;
-            ((float*)dst)[(2 * f + 1) * nn + z] = lo;
+    const int t = threadIdx.x;
+    for (size_t q0 = (size_t)blockIdx.x * LAYOUT_ZONES; q0 < nn; q0 += (size_t)gridDim.x * LAYOUT_ZONES) {
+        const int nz = (int)min((size_t)LAYOUT_ZONES, nn - q0);
+        for (int e = t; e < nz * nf; e += LAYOUT_ZONES) buf[e] = src[q0 * nf + e];
+        __syncthreads();
+        if (t < nz) {
+            const size_t z = plane_index(q0 + t, N, bs, nb);
+            for (int f = 0; f < nf; ++f) {
+                const double v = buf[t * nf + f];
+                if (store == 0) {
+                    ((double*)dst)[f * nn + z] = v;
+                } else {
+                    const float hi = (float)v;
+                    const float lo = (float)(v - (double)hi);
+                    ((float*)dst)[(2 * f) * nn + z] = hi;
+                    ((float*)dst)[(2 * f + 1) * nn + z] = lo;
+                }
+            }
         }
+        __syncthreads();
     }
 }
 
-__global__ void gather_kernel(const void* src, double* dst, int N, int bs, int nb, int nf, int store)
+__global__ void __launch_bounds__(LAYOUT_ZONES) gather_kernel(const void* src, double* dst, int N, int bs, int nb,
+                                                              int nf, int store)
+{
+    __shared__ double buf[LAYOUT_ZONES * 4];
+    const size_t nn = (size_t)N * N;
+    const int t = threadIdx.x;
+    for (size_t q0 = (size_t)blockIdx.x * LAYOUT_ZONES; q0 < nn; q0 += (size_t)gridDim.x * LAYOUT_ZONES) {
+        const int nz = (int)min((size_t)LAYOUT_ZONES, nn - q0);
+        if (t < nz) {
+            const size_t z = plane_index(q0 + t, N, bs, nb);
+            for (int f = 0; f < nf; ++f) {
+                double v;
+                if (store == 0) v = ((const double*)src)[f * nn + z];
+                else v = (double)((const float*)src)[(2 * f) * nn + z] + (double)((const float*)src)[(2 * f + 1) * nn + z];
+                buf[t * nf + f] = v;
+            }
+        }
+        __syncthreads();
+        for (int e = t; e < nz * nf; e += LAYOUT_ZONES) dst[q0 * nf + e] = buf[e];
+        __syncthreads();
+    }
+}
+
+// Launch shape of the layout kernels for one run: LAYOUT_ZONES threads, at
+// most 4096 CTAs striding over the run's zones.
+static unsigned layout_blocks(int N)
 {
     const size_t nn = (size_t)N * N;
-    size_t e0, z0;
-    row_origin(N, bs, nb, nf, e0, z0);
-    for (int t = threadIdx.x; t < bs * nf; t += blockDim.x) {
-        const int lj = zone_of(t, nf), f = t - lj * nf;
-        const size_t z = z0 + lj;
-        double v;
-        if (store == 0) v = ((const double*)src)[f * nn + z];
-        else v = (double)((const float*)src)[(2 * f) * nn + z] + (double)((const float*)src)[(2 * f + 1) * nn + z];
-        dst[e0 + t] = v;
-    }
+    return (unsigned)std::min<size_t>((nn + LAYOUT_ZONES - 1) / LAYOUT_ZONES, 4096);
 }
-
-// Launch shape of the layout kernels for one run.
-static dim3 layout_grid(int nb, int bs) { return dim3((unsigned)(nb * nb), (unsigned)bs); }
-static int layout_threads(int bs, int nf) { return std::min(256, ((bs * nf + 31) / 32) * 32); }
 
 // ---------------------------------------------------------------------------
 // Host-side context.
@@ -693,12 +716,12 @@ extern "C" b2d_status b2d_upload_state(b2d_ctx* ctx, int32_t run, const double* 
     int store = store_of(ctx);
     int grid = 4 * 152;
     CUDA_TRY(cudaMemcpyAsync(ctx->d_staging, cons, n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-    scatter_kernel<<<layout_grid(r.nb, r.bs), layout_threads(r.bs, ctx->nf), 0, ctx->stream>>>(ctx->d_staging, r.slot[ctx->cur], r.N, r.bs, r.nb, ctx->nf, store);
+    scatter_kernel<<<layout_blocks(r.N), LAYOUT_ZONES, 0, ctx->stream>>>(ctx->d_staging, r.slot[ctx->cur], r.N, r.bs, r.nb, ctx->nf, store);
     ctx->launches++;
     CUDA_TRY(cudaGetLastError());
     if (background) {
         CUDA_TRY(cudaMemcpyAsync(ctx->d_staging, background, n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-        scatter_kernel<<<layout_grid(r.nb, r.bs), layout_threads(r.bs, ctx->nf), 0, ctx->stream>>>(ctx->d_staging, r.bg, r.N, r.bs, r.nb, ctx->nf, store);
+        scatter_kernel<<<layout_blocks(r.N), LAYOUT_ZONES, 0, ctx->stream>>>(ctx->d_staging, r.bg, r.N, r.bs, r.nb, ctx->nf, store);
         ctx->launches++;
         CUDA_TRY(cudaGetLastError());
     }
@@ -741,7 +764,7 @@ extern "C" b2d_status b2d_upload_conserved(b2d_ctx* ctx, int32_t run, const doub
         CUDA_TRY(cudaMemcpyAsync(ctx->d_staging, cons, n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
         src = ctx->d_staging;
     }
-    scatter_kernel<<<layout_grid(r.nb, r.bs), layout_threads(r.bs, ctx->nf), 0, ctx->stream>>>(src, r.slot[ctx->cur], r.N, r.bs, r.nb, ctx->nf, store_of(ctx));
+    scatter_kernel<<<layout_blocks(r.N), LAYOUT_ZONES, 0, ctx->stream>>>(src, r.slot[ctx->cur], r.N, r.bs, r.nb, ctx->nf, store_of(ctx));
     ctx->launches++;
     CUDA_TRY(cudaGetLastError());
     b2d_status s = launch_max_speed(ctx, run, ctx->cur);
@@ -784,7 +807,7 @@ extern "C" b2d_status b2d_upload_conserved_async(b2d_ctx* ctx, int32_t run, cons
     CUDA_TRY(cudaMemcpyAsync(ctx->d_in[b], cons, n * sizeof(double), cudaMemcpyHostToDevice, ctx->up_stream));
     CUDA_TRY(cudaEventRecord(ctx->in_copied[b], ctx->up_stream));
     CUDA_TRY(cudaStreamWaitEvent(ctx->stream, ctx->in_copied[b], 0));
-    scatter_kernel<<<layout_grid(r.nb, r.bs), layout_threads(r.bs, ctx->nf), 0, ctx->stream>>>(ctx->d_in[b], r.slot[ctx->cur], r.N, r.bs, r.nb, ctx->nf,
+    scatter_kernel<<<layout_blocks(r.N), LAYOUT_ZONES, 0, ctx->stream>>>(ctx->d_in[b], r.slot[ctx->cur], r.N, r.bs, r.nb, ctx->nf,
                                                        store_of(ctx));
     ctx->launches++;
     CUDA_TRY(cudaGetLastError());
@@ -802,7 +825,7 @@ extern "C" b2d_status b2d_download_async(b2d_ctx* ctx, int32_t run, double* cons
     const int b = (int)(ctx->n_down++ & 1);
     // the staging buffer is free once the copy that last read it has finished
     CUDA_TRY(cudaStreamWaitEvent(ctx->stream, ctx->out_copied[b], 0));
-    gather_kernel<<<layout_grid(r.nb, r.bs), layout_threads(r.bs, ctx->nf), 0, ctx->stream>>>(r.slot[ctx->cur], ctx->d_out[b], r.N, r.bs, r.nb, ctx->nf,
+    gather_kernel<<<layout_blocks(r.N), LAYOUT_ZONES, 0, ctx->stream>>>(r.slot[ctx->cur], ctx->d_out[b], r.N, r.bs, r.nb, ctx->nf,
                                                       store_of(ctx));
     ctx->launches++;
     CUDA_TRY(cudaGetLastError());
@@ -835,7 +858,7 @@ extern "C" b2d_status b2d_download_state(b2d_ctx* ctx, int32_t run, double* cons
     size_t n = (size_t)r.N * r.N * ctx->nf;
     if (cons) {
         double* dst = (double*)mapped_host(cons);
-        gather_kernel<<<layout_grid(r.nb, r.bs), layout_threads(r.bs, ctx->nf), 0, ctx->stream>>>(r.slot[ctx->cur], dst ? dst : ctx->d_staging, r.N, r.bs, r.nb,
+        gather_kernel<<<layout_blocks(r.N), LAYOUT_ZONES, 0, ctx->stream>>>(r.slot[ctx->cur], dst ? dst : ctx->d_staging, r.N, r.bs, r.nb,
                                                          ctx->nf, store_of(ctx));
         ctx->launches++;
         CUDA_TRY(cudaGetLastError());

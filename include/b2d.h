@@ -304,9 +304,9 @@ b2d_status b2d_set_strip_rows(b2d_ctx* ctx, int32_t rows);
 b2d_status b2d_get_strip_rows(const b2d_ctx* ctx, int32_t* rows);
 
 /* Tile autotuner: times every tile shape that divides the block size (width
- * 32..128, or 256 for FP64; height 8..128) and, where the paired FP32 kernel
- * runs, the strip rows that fill one, two or three whole waves of its
- * resident CTAs, over `reps` advances of `fold` steps with CUDA events; keeps
+ * 32..128, or 256 for FP64; height 8..128), the paired FP32 kernel's tiles
+ * that span blocks (128 or 256 columns) and, where that kernel runs, the
+ * strip rows that fill one, two or three whole waves of its resident CTAs, over `reps` advances of `fold` steps with CUDA events; keeps
  * the fastest (b2d_get_tile and b2d_get_strip_rows report it).  The
  * context's state is unchanged. */
 b2d_status b2d_autotune(b2d_ctx* ctx, int32_t fold, int32_t reps, int32_t* tile_w,
