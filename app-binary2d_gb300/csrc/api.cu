@@ -20,7 +20,7 @@
 namespace b2d {
 cudaError_t launch_stage_f64(int nf, const StageArgs& a, int grid, int tw, size_t smem, cudaStream_t s);
 cudaError_t launch_stage_f32(int nf, int store, const StageArgs& a, int grid, int tw, size_t smem, cudaStream_t s);
-int paired_ctas_per_sm(int nruns, int tw);
+int stage_ctas_per_sm(int nf, int store, int nruns, int tw);
 void host_block_vertices(const b2d_config* c, int b, double* xv);
 void host_cell_centers(const b2d_config* c, int b, double* xc);
 }  // namespace b2d
@@ -458,19 +458,23 @@ static void free_ctx(b2d_ctx* ctx)
 
 // Rebuild the tile bookkeeping for the current tile shape and push the run
 // descriptors to the device.
-// The stage kernel the context launches is the paired-column FP32 kernel
-// (launch_stage_f32 makes the same choice).
-static bool paired_kernel(const b2d_ctx* ctx)
+// The stage kernel the context launches takes row chunks: the paired-column
+// kernel or the TMA-staged one (launch_stage_f32 makes the same choice), not
+// the FP64 or the generic kernel.
+static bool chunk_kernel(const b2d_ctx* ctx)
 {
-    return ctx->precision == B2D_PREC_FP32_COMP && ctx->nf == 3 && (ctx->tw == 64 || ctx->tw == 128 || ctx->tw == 256);
+    if (ctx->precision == B2D_PREC_FP64) return false;
+    if (ctx->precision == B2D_PREC_FP32_COMP && ctx->nf == 3 && (ctx->tw == 64 || ctx->tw == 128 || ctx->tw == 256))
+        return true;
+    return ctx->tw % 32 == 0 && ctx->tw <= 128;
 }
 
 // Row chunks per column strip of a run: block-aligned tiles of height th, or,
-// with strip rows set and the paired kernel launched, ceil(N / rows) chunks
-// that may cross one block boundary each.
+// with strip rows set and a chunk-taking kernel launched, ceil(N / rows)
+// chunks that may cross one block boundary each.
 static int row_chunks(const b2d_ctx* ctx, const RunHost& r)
 {
-    if (ctx->strip_rows > 0 && paired_kernel(ctx)) return (r.N + ctx->strip_rows - 1) / ctx->strip_rows;
+    if (ctx->strip_rows > 0 && chunk_kernel(ctx)) return (r.N + ctx->strip_rows - 1) / ctx->strip_rows;
     return r.N / ctx->th;
 }
 
@@ -1586,7 +1590,7 @@ static b2d_status time_tile(b2d_ctx* ctx, int fold, int reps, double* ms)
     return B2D_OK;
 }
 
-// Strip rows for the paired kernel at the context's tile width: for the
+// Strip rows for the chunk-taking kernel at the context's tile width: for the
 // fewest whole waves of resident CTAs that chunks of at most a block's rows
 // fill, and the next two, the shortest chunks that still fit in them.
 static std::vector<int> strip_row_candidates(const b2d_ctx* ctx)
@@ -1595,7 +1599,7 @@ static std::vector<int> strip_row_candidates(const b2d_ctx* ctx)
     int dev = 0, sms = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return out;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return out;
-    const int per_sm = paired_ctas_per_sm(ctx->nruns, ctx->tw);
+    const int per_sm = stage_ctas_per_sm(ctx->nf, store_of(ctx), ctx->nruns, ctx->tw);
     if (sms <= 0 || per_sm <= 0) return out;
     const long long slots = (long long)sms * per_sm;
     int min_bs = 1 << 30;
@@ -1639,15 +1643,15 @@ extern "C" b2d_status b2d_autotune(b2d_ctx* ctx, int32_t fold, int32_t reps, int
             if (ms < best) { best = ms; best_w = w; best_h = h; }
         }
     }
-    // row chunks of the paired kernel, at each of its tile widths
-    for (int w : {64, 128, 256}) {
+    // row chunks of the FP32 kernels, at each tile width that takes them
+    for (int w : {32, 64, 128, 256}) {
         int h = 0;
         for (int hh : {64, 32, 16, 8})
             if (!h && tile_ok(ctx, w, hh)) h = hh;
         if (!h) continue;
         ctx->tw = w;
         ctx->th = h;
-        if (!paired_kernel(ctx)) continue;
+        if (!chunk_kernel(ctx)) continue;
         for (int rows : strip_row_candidates(ctx)) {
             ctx->strip_rows = rows;
             st = sync_rundev(ctx);

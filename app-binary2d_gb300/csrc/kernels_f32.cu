@@ -1,9 +1,9 @@
 // kernels_f32.cu — FP32-stencil stage kernels over FP64 state (store 0) or
-// compensated FP32 state (store 1).  Isothermal compensated tiles whose width
-// is a multiple of 64 run the paired-column kernel of stage3.cuh; other tiles
-// whose width is a multiple of 32 run the TMA-staged kernel of stage2.cuh;
-// narrower tiles (blocks of fewer than 32 zones) run the generic kernel of
-// stage.cuh.
+// compensated FP32 state (store 1).  Isothermal compensated tiles 64, 128 or
+// 256 columns wide run the paired-column kernel of stage3.cuh; other tiles
+// whose width is a multiple of 32 (at most 128) run the TMA-staged kernel of
+// stage2.cuh; narrower tiles (blocks of fewer than 32 zones) run the generic
+// kernel of stage.cuh.  The first two take row chunks across block rows.
 #include "kernels.inc"
 #include "stage3.cuh"
 
@@ -48,19 +48,38 @@ static cudaError_t launch_three_impl(const StageArgs& a, int grid, int tw, cudaS
     return cudaGetLastError();
 }
 
-// Resident CTAs per SM of the paired kernel for a tile width (the autotuner
-// sizes row chunks to whole waves with it).
-int paired_ctas_per_sm(int nruns, int tw)
+template <int NF, int STORE>
+static int two_ctas_per_sm(int nruns, int tw)
 {
-    const size_t smem = s3_smem_bytes(tw);
     int n = 0;
-    const bool wide = tw == 256;
+    const size_t smem = s2_smem_bytes(NF, STORE, tw);
     cudaError_t e = nruns == 1
-        ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-              &n, wide ? stage3_kernel<true, true> : stage3_kernel<true, false>, tw / 2 + 32, smem)
-        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-              &n, wide ? stage3_kernel<false, true> : stage3_kernel<false, false>, tw / 2 + 32, smem);
+        ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, stage2_kernel<NF, STORE, true>, tw + 32, smem)
+        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, stage2_kernel<NF, STORE, false>, tw + 32, smem);
     return e == cudaSuccess ? n : 0;
+}
+
+// Resident CTAs per SM of the FP32 stage kernel that launch_stage_f32 runs for
+// a tile width (the autotuner sizes row chunks to whole waves with it); 0 for
+// the generic kernel, which takes no row chunks.
+int stage_ctas_per_sm(int nf, int store, int nruns, int tw)
+{
+    int n = 0;
+    if (nf == 3 && store == 1 && (tw == 64 || tw == 128 || tw == 256)) {
+        const size_t smem = s3_smem_bytes(tw);
+        const bool wide = tw == 256;
+        cudaError_t e = nruns == 1
+            ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                  &n, wide ? stage3_kernel<true, true> : stage3_kernel<true, false>, tw / 2 + 32, smem)
+            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                  &n, wide ? stage3_kernel<false, true> : stage3_kernel<false, false>, tw / 2 + 32, smem);
+        return e == cudaSuccess ? n : 0;
+    }
+    if (tw % 32 == 0 && tw <= 128) {
+        if (nf == 3) return store == 0 ? two_ctas_per_sm<3, 0>(nruns, tw) : two_ctas_per_sm<3, 1>(nruns, tw);
+        return store == 0 ? two_ctas_per_sm<4, 0>(nruns, tw) : two_ctas_per_sm<4, 1>(nruns, tw);
+    }
+    return 0;
 }
 
 cudaError_t launch_stage_f32(int nf, int store, const StageArgs& a, int grid, int tw, size_t smem, cudaStream_t s)

@@ -467,6 +467,14 @@ __device__ __forceinline__ bool source_terms(const DevParamsT<R>& P, const Binar
         if constexpr (std::is_same<R, double>::value) e0 = p0[3] / p0[0] / P.gm1;
         else e0 = dvd(p0[3], p0[0]) * P.inv_gm1;
         R ec;
+        // FP32: the cooled minus the initial specific energy, formed directly
+        // (e0 (exp(-c) - 1), e0 ((1 + x)^(-1/3) - 1) through expm1 and log1p):
+        // as a difference of two near-equal energies it loses ~1e-7 / (c or x)
+        // of its value, 1e-3 for changes of 1e-4 per stage.  The cooling item's
+        // mass and momentum are zero in FP32: uc - u there is only the rounding
+        // of a prim -> cons round trip (1e-16 of rho v in FP64, 1e-7 in FP32,
+        // more than a weak cooling's energy term)
+        R dec = R(0);
         if (P.cooling_kind == 1) {
             // β-cooling (not in the reference): e → e·exp(-Ω dt / β)
             R d1x = x - b.p1.x, d1y = y - b.p1.y, d2x = x - b.p2.x, d2y = y - b.p2.y;
@@ -479,7 +487,10 @@ __device__ __forceinline__ bool source_terms(const DevParamsT<R>& P, const Binar
                 om = sqrtf(b.p1.m * q1 * q1 * q1 + b.p2.m * q2 * q2 * q2);
             }
             if constexpr (std::is_same<R, double>::value) ec = e0 * exp(-om * dt / P.cool_beta);
-            else ec = e0 * __expf(-om * dt * P.inv_cool_beta);
+            else {
+                dec = e0 * expm1f(-om * dt * P.inv_cool_beta);
+                ec = e0 + dec;
+            }
         } else {
             R f = R(1);
             if (P.cooling_slow_start) {
@@ -490,12 +501,21 @@ __device__ __forceinline__ bool source_terms(const DevParamsT<R>& P, const Binar
             for (int k = 0; k < P.density_index; ++k) rho_n *= p0[0];
             R a = dvd(R(P.cool_coef), rho_n) * f;
             if constexpr (std::is_same<R, double>::value) ec = e0 * pow(1.0 + 3.0 * a * (e0 * e0 * e0) * dt, -1.0 / 3.0);
-            else ec = e0 * __powf(1.0f + 3.0f * a * (e0 * e0 * e0) * dt, -1.0f / 3.0f);
+            else {
+                dec = e0 * expm1f(log1pf(3.0f * a * (e0 * e0 * e0) * dt) * (-1.0f / 3.0f));
+                ec = e0 + dec;
+            }
         }
         if (P.has_mach_ceiling) {
             R ek = R(0.5) * (p0[1] * p0[1] + p0[2] * p0[2]);
             if constexpr (std::is_same<R, double>::value) ec = fmax(ec, 2.0 * ek / g / P.gm1 / P.mach_ceiling2);
-            else ec = fmaxf(ec, ek * P.k_mach_ceiling);
+            else {
+                const R ecm = fmaxf(ec, ek * P.k_mach_ceiling);
+                if (ecm != ec) {   // the ceiling binds (or ec was not a number)
+                    dec = ecm - e0;
+                    ec = ecm;
+                }
+            }
         }
         R pc[4] = {p0[0], p0[1], p0[2], p0[0] * ec * R(P.gm1)};
         R uc[4];
@@ -531,7 +551,8 @@ __device__ __forceinline__ bool source_terms(const DevParamsT<R>& P, const Binar
             it[SINK1 * 4 + k] = s1[k] * dt;
             it[SINK2 * 4 + k] = s2v[k] * dt;
             it[BUFFER * 4 + k] = (u[k] - u0[k]) * kb;
-            it[COOLING * 4 + k] = uc[k] - u[k];
+            if constexpr (std::is_same<R, double>::value) it[COOLING * 4 + k] = uc[k] - u[k];
+            else it[COOLING * 4 + k] = k == 3 ? p0[0] * dec : R(0);
             it[FAKE_MASS * 4 + k] = R(0);
         }
     }

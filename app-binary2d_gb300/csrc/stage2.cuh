@@ -250,6 +250,74 @@ __device__ __forceinline__ const DevParamsF& params_for(const StageArgs& a, cons
     else return shared_copy;
 }
 
+constexpr int PIECE_MAX_THREADS = 128;   // interior threads of the widest paired tile (256 columns)
+
+// One ledger piece of a tile (its columns in block (brow, bj)), by one warp
+// after the row loop (stage2 and stage3 kernels): sums over the bank rows of
+// the nw interior warps over those columns, the piece's slot in the block's partials, and the fold of
+// the block's pieces (in piece order) by the block's last piece.  acc (a
+// crossing tile's first piece) holds group 0 per thread of those warps, to be
+// reduced here first.  Out of line, so that it does not weigh on the row
+// loop's register allocation; no CTA barrier, so that warps can flush
+// several pieces at once.
+template <int NF>
+__device__ __noinline__ void flush_piece(const RunDev& rd, int brow, int bj, int lslot, int TW, float (*bank)[32],
+                                         int nw, const float (*acc)[PIECE_MAX_THREADS], int in_slot, int base_slot,
+                                         int out_slot, int stage, double bf)
+{
+    constexpr int NL = NITEMS * NF;
+    const int lane = threadIdx.x & 31;
+    if (acc) {
+        float v0[8];
+#pragma unroll
+        for (int m = 0; m < 7; ++m) {
+            v0[m] = 0.0f;
+            for (int w = 0; w < nw; ++w) v0[m] += acc[m][lane + 32 * w];
+        }
+        v0[7] = 0.0f;
+        const float s0 = warp_sum_items<8>(v0, lane);
+        const int slot0 = group_writer_slot<NF, 0>(lane);
+        if (slot0 >= 0) bank[0][slot0] += s0;
+        __syncwarp();
+    }
+    const int bs = rd.bs, nc = rd.tiles_i, per_row = max(bs / TW, 1);
+    const int ti = ((int)blockIdx.x - rd.tile_base) / rd.tiles_j;
+    const int block = brow * rd.nb + bj;
+    const int piece = (ti - chunk_of_row(brow * bs, rd.N, nc)) * per_row + lslot;
+    const int pieces = chunks_in_block_row(brow, bs, rd.N, nc) * per_row;
+    if (lane < NL) {
+        int j = 0;
+        bool live = false;
+        for (int k2 = 0; k2 < NL; ++k2) {
+            if (k2 == lane) { live = item_live<NF>(k2); break; }
+            if (item_live<NF>(k2)) ++j;
+        }
+        double s = 0.0;
+        if (live)
+            for (int w = 0; w < nw; ++w) s += (double)bank[w][j];
+        rd.partial[((size_t)block * rd.tiles_per_block + piece) * NL + lane] = s;
+        __threadfence();   // visible before the counter below counts this piece
+    }
+    __syncwarp();
+    unsigned last = 0;
+    if (lane == 0) last = atomicAdd(rd.counter + block, 1u) == (unsigned)pieces - 1;
+    last = __shfl_sync(0xffffffffu, last, 0);
+    if (!last) return;
+    __threadfence();
+    if (lane < NL) {
+        const double area = (double)rd.p.dx * rd.p.dx;
+        double s = 0.0;
+        for (int q = 0; q < pieces; ++q)
+            s += __ldcg(rd.partial + ((size_t)block * rd.tiles_per_block + q) * NL + lane);
+        double v = __ldcg(rd.ledger[in_slot] + (size_t)block * NL + lane) + s * area;
+        if (base_slot >= 0) v = v * (-bf + 1.0) + __ldcg(rd.ledger[base_slot] + (size_t)block * NL + lane) * bf;
+        rd.ledger[out_slot][(size_t)block * NL + lane] = v;
+        // the block's ds·dx·dy of this stage, for the orbital-element ledger
+        if (rd.stage_ds) rd.stage_ds[((size_t)stage * rd.nblocks + block) * NL + lane] = s * area;
+    }
+    if (lane == 0) rd.counter[block] = 0u;
+}
+
 template <int NF, int STORE, bool SINGLE>
 __global__ void __launch_bounds__(160, (NF == 3 && STORE == 1) ? 4 : 3) stage2_kernel(StageArgs a)
 {
@@ -259,7 +327,6 @@ __global__ void __launch_bounds__(160, (NF == 3 && STORE == 1) ? 4 : 3) stage2_k
     constexpr int NL = NITEMS * NF;
 
     const int TW = blockDim.x - 32;
-    const int TH = a.th;
     const int t = threadIdx.x;
     const int SW = TW + 2 * H;
 
@@ -295,10 +362,16 @@ __global__ void __launch_bounds__(160, (NF == 3 && STORE == 1) ? 4 : 3) stage2_k
     const size_t nn = (size_t)N * N;
     const int lt = g - rd.tile_base;
     const int tj = lt % rd.tiles_j, ti = lt / rd.tiles_j;
-    const int i0 = ti * TH, j0 = tj * TW;
-    const int bi = i0 / bs, bj = j0 / bs, li0 = i0 % bs, lj0 = j0 % bs;
-    const int block = bi * rd.nb + bj;
-    const int tib = (li0 / TH) * (bs / TW) + lj0 / TW;
+    // rows [i0, i0 + TH): row chunk ti of C (chunk_start, runtime.cuh); a chunk
+    // of at most bs rows lies in one block row, or in two from its row rb, and
+    // its ledger piece in the last of them is the tile's main piece
+    const int C = rd.tiles_i;
+    const int i0 = chunk_start(ti, N, C), TH = chunk_start(ti + 1, N, C) - i0, j0 = tj * TW;
+    const int bj = j0 / bs, lj0 = j0 % bs;
+    const int rb = min(bs - i0 % bs, TH);
+    const int bl = (i0 + TH - 1) / bs;
+    const int block = bl * rd.nb + bj;
+    const int tib = (ti - chunk_of_row(bl * bs, N, C)) * (bs / TW) + lj0 / TW;
     const bool has_base = a.base_slot >= 0;
 
     const E* uin = (const E*)rd.slot[a.in_slot];
@@ -403,7 +476,7 @@ __global__ void __launch_bounds__(160, (NF == 3 && STORE == 1) ? 4 : 3) stage2_k
     // positions of this thread's column: zone centre y and left y-face
     const float yc_own = interior ? xc[j0 + c] : 0.0f;
     const float yv_own = has_fy ? xv[bj * (bs + 1) + lj0 + c] : 0.0f;
-    const float* xv_row = xv + bi * (bs + 1) + li0;    // x of face (i0 + r) - 1/2 is xv_row[r]
+    const float* xv_row = rd.xvgf + i0;                // x of face (i0 + r) - 1/2 is xv_row[r]
     const float* xc_row = xc + i0;
     // column parts (dy^2 + s^2) of the body distances of this column's faces
     float cyv1 = 0.0f, cyv2 = 0.0f, cyc1 = 0.0f, cyc2 = 0.0f;
@@ -421,9 +494,9 @@ __global__ void __launch_bounds__(160, (NF == 3 && STORE == 1) ? 4 : 3) stage2_k
     // source ledger: per-warp accumulators of the live items, one lane each
     constexpr int NLIVE = live_items<NF>();
     static_assert(group_size<NF, 0>() + group_size<NF, 1>() + group_size<NF, 2>() == NLIVE, "ledger groups");
-    __shared__ float sLed[4][32];
+    __shared__ float sLed[4][32], sLedA[4][32];   // [warp][item slot]: main piece, a crossing tile's first piece
     const int lane = t & 31, warp = t >> 5;
-    if (t < 128) sLed[t >> 5][t & 31] = 0.0f;
+    if (t < 128) sLed[t >> 5][t & 31] = sLedA[t >> 5][t & 31] = 0.0f;
     const int slot0 = group_writer_slot<NF, 0>(lane);
     const int slot1 = group_writer_slot<NF, 1>(lane);
     const int slot2 = group_writer_slot<NF, 2>(lane);
@@ -605,6 +678,11 @@ __global__ void __launch_bounds__(160, (NF == 3 && STORE == 1) ? 4 : 3) stage2_k
                     reduce_group<NF, 0>(it, lane, slot0, sLed[warp]);
                     if (sinks_on) reduce_group<NF, 1>(it, lane, slot1, sLed[warp]);
                     if (fake_on) reduce_group<NF, 2>(it, lane, slot2, sLed[warp]);
+                    if (ru == rb - 1 && rb < TH) {   // the first piece's last row: set its sums aside
+                        __syncwarp();
+                        sLedA[warp][lane] = sLed[warp][lane];
+                        sLed[warp][lane] = 0.0f;
+                    }
                 }
                 if (want_amax && up_ok) amax = fmaxf(max_signal_speed<NF, float>(P, uc), amax);
             }
@@ -630,23 +708,9 @@ __global__ void __launch_bounds__(160, (NF == 3 && STORE == 1) ? 4 : 3) stage2_k
         __syncthreads();
     }
 
-    // ---- per-tile ledger and max speed (deterministic tree over the CTA) -------------
+    // ---- max speed of the tile (deterministic tree over the CTA; the ring is idle) --
     double* red = (double*)smem_raw;
     const int NT = blockDim.x;
-    if (t < NL) {
-        // live item index of ledger slot t, summed over the interior warps in order
-        int j = 0;
-        bool live = false;
-        for (int k2 = 0; k2 < NL; ++k2) {
-            if (k2 == t) { live = item_live<NF>(k2); break; }
-            if (item_live<NF>(k2)) ++j;
-        }
-        double s = 0.0;
-        if (live)
-            for (int w = 0; w < TW / 32; ++w) s += (double)sLed[w][j];
-        rd.partial[((size_t)block * rd.tiles_per_block + tib) * NL + t] = s;
-        __threadfence();   // visible before the counter below counts this tile
-    }
     if (a.amax_flag) {
         red[t] = (double)amax;
         __syncthreads();
@@ -658,32 +722,16 @@ __global__ void __launch_bounds__(160, (NF == 3 && STORE == 1) ? 4 : 3) stage2_k
     }
     if (t == 0 && timeout) atomicOr(a.timeout_flag, 1u);
 
-    __shared__ int is_last;
+    // ---- ledger pieces: the main piece by warp 0, a crossing tile's first piece (the
+    // block row above) by warp 1, at once ----------------------------------------
     __syncthreads();
-    if (t == 0) {
-        __threadfence();
-        unsigned prev = atomicAdd(rd.counter + block, 1u);
-        is_last = (prev == (unsigned)rd.tiles_per_block - 1);
-    }
-    __syncthreads();
-    if (is_last) {
-        __threadfence();
-        const double area = (double)rd.p.dx * rd.p.dx;
-        const double* lin = rd.ledger[a.in_slot] + (size_t)block * NL;
-        const double* lbase = has_base ? rd.ledger[a.base_slot] + (size_t)block * NL : nullptr;
-        double* lout = rd.ledger[a.out_slot] + (size_t)block * NL;
-        for (int k = t; k < NL; k += NT) {
-            double s = 0.0;
-            for (int q = 0; q < rd.tiles_per_block; ++q)
-                s += __ldcg(rd.partial + ((size_t)block * rd.tiles_per_block + q) * NL + k);
-            double v = __ldcg(lin + k) + s * area;
-            if (lbase) v = v * (-a.bf + 1.0) + __ldcg(lbase + k) * a.bf;
-            lout[k] = v;
-            // the block's ds·dx·dy of this stage, for the orbital-element ledger
-            if (rd.stage_ds) rd.stage_ds[((size_t)a.stage * rd.nblocks + block) * NL + k] = s * area;
-        }
-        if (t == 0) rd.counter[block] = 0u;
-    }
+    const int brow = block / rd.nb, lslot = tib % (rd.bs / TW);
+    if (warp == 0)
+        flush_piece<NF>(rd, brow, block - brow * rd.nb, lslot, TW, sLed, TW / 32, nullptr, a.in_slot, a.base_slot,
+                        a.out_slot, a.stage, a.bf);
+    else if (warp == 1 && rb < TH)
+        flush_piece<NF>(rd, brow - 1, block - brow * rd.nb, lslot, TW, sLedA, TW / 32, nullptr, a.in_slot,
+                        a.base_slot, a.out_slot, a.stage, a.bf);
 }
 
 }  // namespace b2d

@@ -160,79 +160,12 @@ __device__ __forceinline__ void face_flux2(const DevParamsF& P, const Binary<flo
 constexpr int S3_DEPTH = 1;
 constexpr int S3_SLOTS = S3_DEPTH + 4;   // stencil ring: a row is read again 3 rows after it lands
 constexpr int S3_USLOTS = S3_DEPTH + 1;  // update ring
-constexpr int S3_MAX_TP = 128;           // interior threads of the widest tile (256 columns)
 
 __host__ __device__ inline int s3_smem_bytes(int tw)
 {
     int slots = S3_SLOTS * s2_slot_bytes(3, 1, tw) + S3_USLOTS * s2_uslot_bytes(3, 1, tw);
     int exch = 16 * (2 * (tw + 4) + 3 * 2 * (tw + 4) + 2 * (tw + 2));
     return slots + exch + 8 * (S3_SLOTS + S3_USLOTS);
-}
-
-// One ledger piece of a tile (its columns in block (brow, bj)), by one warp
-// after the row loop: sums over the bank rows of the nw interior warps over
-// those columns, the piece's slot in the block's partials, and the fold of
-// the block's pieces (in piece order) by the block's last piece.  acc (a
-// crossing tile's first piece) holds group 0 per thread of those warps, to be
-// reduced here first.  Out of line, so that it does not weigh on the row
-// loop's register allocation; no CTA barrier, so that warps can flush
-// several pieces at once.
-template <int NF>
-__device__ __noinline__ void flush_piece(const RunDev& rd, int brow, int bj, int lslot, int TW, float (*bank)[32],
-                                         int nw, const float (*acc)[S3_MAX_TP], int in_slot, int base_slot,
-                                         int out_slot, int stage, double bf)
-{
-    constexpr int NL = NITEMS * NF;
-    const int lane = threadIdx.x & 31;
-    if (acc) {
-        float v0[8];
-#pragma unroll
-        for (int m = 0; m < 7; ++m) {
-            v0[m] = 0.0f;
-            for (int w = 0; w < nw; ++w) v0[m] += acc[m][lane + 32 * w];
-        }
-        v0[7] = 0.0f;
-        const float s0 = warp_sum_items<8>(v0, lane);
-        const int slot0 = group_writer_slot<NF, 0>(lane);
-        if (slot0 >= 0) bank[0][slot0] += s0;
-        __syncwarp();
-    }
-    const int bs = rd.bs, nc = rd.tiles_i, per_row = max(bs / TW, 1);
-    const int ti = ((int)blockIdx.x - rd.tile_base) / rd.tiles_j;
-    const int block = brow * rd.nb + bj;
-    const int piece = (ti - chunk_of_row(brow * bs, rd.N, nc)) * per_row + lslot;
-    const int pieces = chunks_in_block_row(brow, bs, rd.N, nc) * per_row;
-    if (lane < NL) {
-        int j = 0;
-        bool live = false;
-        for (int k2 = 0; k2 < NL; ++k2) {
-            if (k2 == lane) { live = item_live<NF>(k2); break; }
-            if (item_live<NF>(k2)) ++j;
-        }
-        double s = 0.0;
-        if (live)
-            for (int w = 0; w < nw; ++w) s += (double)bank[w][j];
-        rd.partial[((size_t)block * rd.tiles_per_block + piece) * NL + lane] = s;
-        __threadfence();   // visible before the counter below counts this piece
-    }
-    __syncwarp();
-    unsigned last = 0;
-    if (lane == 0) last = atomicAdd(rd.counter + block, 1u) == (unsigned)pieces - 1;
-    last = __shfl_sync(0xffffffffu, last, 0);
-    if (!last) return;
-    __threadfence();
-    if (lane < NL) {
-        const double area = (double)rd.p.dx * rd.p.dx;
-        double s = 0.0;
-        for (int q = 0; q < pieces; ++q)
-            s += __ldcg(rd.partial + ((size_t)block * rd.tiles_per_block + q) * NL + lane);
-        double v = __ldcg(rd.ledger[in_slot] + (size_t)block * NL + lane) + s * area;
-        if (base_slot >= 0) v = v * (-bf + 1.0) + __ldcg(rd.ledger[base_slot] + (size_t)block * NL + lane) * bf;
-        rd.ledger[out_slot][(size_t)block * NL + lane] = v;
-        // the block's ds·dx·dy of this stage, for the orbital-element ledger
-        if (rd.stage_ds) rd.stage_ds[((size_t)stage * rd.nblocks + block) * NL + lane] = s * area;
-    }
-    if (lane == 0) rd.counter[block] = 0u;
 }
 
 // WIDE: 256-column tiles over two 128-column blocks (or one 256-column block),
@@ -395,7 +328,7 @@ __global__ void __launch_bounds__(WIDE ? 160 : 96, WIDE ? 2 : 4) stage3_kernel(S
     static_assert(group_size<NF, 0>() + group_size<NF, 1>() + group_size<NF, 2>() == NLIVE, "ledger groups");
     // [warp][item slot] of the main piece and of a crossing tile's first piece;
     // group 0 of the first piece per thread
-    __shared__ float sLed[4][32], sLedA[4][32], sAccA[7][S3_MAX_TP];
+    __shared__ float sLed[4][32], sLedA[4][32], sAccA[7][PIECE_MAX_THREADS];
     const int lane = t & 31, warp = t >> 5;
     if (t < 128) sLed[t >> 5][t & 31] = sLedA[t >> 5][t & 31] = 0.0f;
     const int slot0 = group_writer_slot<NF, 0>(lane);
@@ -733,7 +666,7 @@ __global__ void __launch_bounds__(WIDE ? 160 : 96, WIDE ? 2 : 4) stage3_kernel(S
                             a.out_slot, a.stage, a.bf);
         else
             flush_piece<NF>(rd, brow - 1, bcol + c, lslot, TW, sLedA + c * wpc, wpc,
-                            (const float (*)[S3_MAX_TP])(&sAccA[0][c * wpc * 32]), a.in_slot, a.base_slot,
+                            (const float (*)[PIECE_MAX_THREADS])(&sAccA[0][c * wpc * 32]), a.in_slot, a.base_slot,
                             a.out_slot, a.stage, a.bf);
     }
 }

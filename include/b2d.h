@@ -291,8 +291,9 @@ b2d_status b2d_initial_state(const b2d_config* cfg, const b2d_disk_model* model,
 b2d_status b2d_set_tile(b2d_ctx* ctx, int32_t tile_w, int32_t tile_h);
 b2d_status b2d_get_tile(const b2d_ctx* ctx, int32_t* tile_w, int32_t* tile_h);
 
-/* Row chunks of the paired-column FP32 stage kernel (precision FP32_COMP,
- * isothermal, tile width 64, 128 or 256).  rows > 0: every column strip of tile
+/* Row chunks of the FP32 stage kernels (the paired-column kernel: FP32_COMP,
+ * isothermal, tile width 64, 128 or 256; the TMA-staged kernel: FP32 tiles
+ * whose width is a multiple of 32, at most 128).  rows > 0: every column strip of tile
  * width is covered in ceil(N / rows) row chunks of near-equal height (at most
  * `rows`; 8 <= rows <= block_size), each of which may cross one block
  * boundary, so that the stage's CTAs can fill whole waves of the GPU; the
