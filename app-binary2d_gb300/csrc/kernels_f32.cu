@@ -1,6 +1,6 @@
 // kernels_f32.cu — FP32-stencil stage kernels over FP64 state (store 0) or
-// compensated FP32 state (store 1).  Isothermal compensated tiles 64, 128 or
-// 256 columns wide run the paired-column kernel of stage3.cuh; other tiles
+// compensated FP32 state (store 1).  Isothermal compensated tiles 64, 128,
+// 256 or 512 columns wide run the paired-column kernel of stage3.cuh; other tiles
 // whose width is a multiple of 32 (at most 128) run the TMA-staged kernel of
 // stage2.cuh; narrower tiles (blocks of fewer than 32 zones) run the generic
 // kernel of stage.cuh.  The first two take row chunks across block rows.
@@ -33,10 +33,10 @@ static cudaError_t launch_two(const StageArgs& a, int grid, int tw, cudaStream_t
     return launch_two_impl<NF, STORE, false>(a, grid, tw, s);
 }
 
-template <bool SINGLE, bool WIDE>
+template <bool SINGLE, int TWMAX>
 static cudaError_t launch_three_impl(const StageArgs& a, int grid, int tw, cudaStream_t s)
 {
-    auto k = stage3_kernel<SINGLE, WIDE>;
+    auto k = stage3_kernel<SINGLE, TWMAX>;
     size_t smem = s3_smem_bytes(tw);
     static size_t configured = 0;
     if (smem > configured) {
@@ -65,14 +65,15 @@ static int two_ctas_per_sm(int nruns, int tw)
 int stage_ctas_per_sm(int nf, int store, int nruns, int tw)
 {
     int n = 0;
-    if (nf == 3 && store == 1 && (tw == 64 || tw == 128 || tw == 256)) {
+    if (nf == 3 && store == 1 && (tw == 64 || tw == 128 || tw == 256 || tw == 512)) {
         const size_t smem = s3_smem_bytes(tw);
-        const bool wide = tw == 256;
-        cudaError_t e = nruns == 1
-            ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                  &n, wide ? stage3_kernel<true, true> : stage3_kernel<true, false>, tw / 2 + 32, smem)
-            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                  &n, wide ? stage3_kernel<false, true> : stage3_kernel<false, false>, tw / 2 + 32, smem);
+        void (*k)(StageArgs);
+        if (tw <= 128) k = nruns == 1 ? stage3_kernel<true, 128> : stage3_kernel<false, 128>;
+        else if (tw == 256) k = nruns == 1 ? stage3_kernel<true, 256> : stage3_kernel<false, 256>;
+        else k = nruns == 1 ? stage3_kernel<true, 512> : stage3_kernel<false, 512>;
+        // the opt-in above 48 KB of dynamic shared memory, as at launch
+        if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, tw / 2 + 32, smem);
         return e == cudaSuccess ? n : 0;
     }
     if (tw % 32 == 0 && tw <= 128) {
@@ -85,11 +86,14 @@ int stage_ctas_per_sm(int nf, int store, int nruns, int tw)
 cudaError_t launch_stage_f32(int nf, int store, const StageArgs& a, int grid, int tw, size_t smem, cudaStream_t s)
 {
     if (nf == 3 && store == 1 && (tw == 64 || tw == 128))
-        return a.nruns == 1 ? launch_three_impl<true, false>(a, grid, tw, s)
-                            : launch_three_impl<false, false>(a, grid, tw, s);
+        return a.nruns == 1 ? launch_three_impl<true, 128>(a, grid, tw, s)
+                            : launch_three_impl<false, 128>(a, grid, tw, s);
     if (nf == 3 && store == 1 && tw == 256)
-        return a.nruns == 1 ? launch_three_impl<true, true>(a, grid, tw, s)
-                            : launch_three_impl<false, true>(a, grid, tw, s);
+        return a.nruns == 1 ? launch_three_impl<true, 256>(a, grid, tw, s)
+                            : launch_three_impl<false, 256>(a, grid, tw, s);
+    if (nf == 3 && store == 1 && tw == 512)
+        return a.nruns == 1 ? launch_three_impl<true, 512>(a, grid, tw, s)
+                            : launch_three_impl<false, 512>(a, grid, tw, s);
     if (tw % 32 == 0 && tw <= 128) {
         if (nf == 3) return store == 0 ? launch_two<3, 0>(a, grid, tw, s) : launch_two<3, 1>(a, grid, tw, s);
         return store == 0 ? launch_two<4, 0>(a, grid, tw, s) : launch_two<4, 1>(a, grid, tw, s);

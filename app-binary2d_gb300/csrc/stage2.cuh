@@ -250,8 +250,6 @@ __device__ __forceinline__ const DevParamsF& params_for(const StageArgs& a, cons
     else return shared_copy;
 }
 
-constexpr int PIECE_MAX_THREADS = 128;   // interior threads of the widest paired tile (256 columns)
-
 // One ledger piece of a tile (its columns in block (brow, bj)), by one warp
 // after the row loop (stage2 and stage3 kernels): sums over the bank rows of
 // the nw interior warps over those columns, the piece's slot in the block's partials, and the fold of
@@ -262,7 +260,7 @@ constexpr int PIECE_MAX_THREADS = 128;   // interior threads of the widest paire
 // several pieces at once.
 template <int NF>
 __device__ __noinline__ void flush_piece(const RunDev& rd, int brow, int bj, int lslot, int TW, float (*bank)[32],
-                                         int nw, const float (*acc)[PIECE_MAX_THREADS], int in_slot, int base_slot,
+                                         int nw, const float* acc, int acc_stride, int in_slot, int base_slot,
                                          int out_slot, int stage, double bf)
 {
     constexpr int NL = NITEMS * NF;
@@ -272,7 +270,7 @@ __device__ __noinline__ void flush_piece(const RunDev& rd, int brow, int bj, int
 #pragma unroll
         for (int m = 0; m < 7; ++m) {
             v0[m] = 0.0f;
-            for (int w = 0; w < nw; ++w) v0[m] += acc[m][lane + 32 * w];
+            for (int w = 0; w < nw; ++w) v0[m] += acc[m * acc_stride + lane + 32 * w];
         }
         v0[7] = 0.0f;
         const float s0 = warp_sum_items<8>(v0, lane);
@@ -727,10 +725,10 @@ __global__ void __launch_bounds__(160, (NF == 3 && STORE == 1) ? 4 : 3) stage2_k
     __syncthreads();
     const int brow = block / rd.nb, lslot = tib % (rd.bs / TW);
     if (warp == 0)
-        flush_piece<NF>(rd, brow, block - brow * rd.nb, lslot, TW, sLed, TW / 32, nullptr, a.in_slot, a.base_slot,
+        flush_piece<NF>(rd, brow, block - brow * rd.nb, lslot, TW, sLed, TW / 32, nullptr, 0, a.in_slot, a.base_slot,
                         a.out_slot, a.stage, a.bf);
     else if (warp == 1 && rb < TH)
-        flush_piece<NF>(rd, brow - 1, block - brow * rd.nb, lslot, TW, sLedA, TW / 32, nullptr, a.in_slot,
+        flush_piece<NF>(rd, brow - 1, block - brow * rd.nb, lslot, TW, sLedA, TW / 32, nullptr, 0, a.in_slot,
                         a.base_slot, a.out_slot, a.stage, a.bf);
 }
 

@@ -168,11 +168,13 @@ __host__ __device__ inline int s3_smem_bytes(int tw)
     return slots + exch + 8 * (S3_SLOTS + S3_USLOTS);
 }
 
-// WIDE: 256-column tiles over two 128-column blocks (or one 256-column block),
-// 4 interior warps to each halo warp, 2 CTAs per SM; otherwise 64- or
-// 128-column tiles, 4 CTAs per SM.
-template <bool SINGLE, bool WIDE>
-__global__ void __launch_bounds__(WIDE ? 160 : 96, WIDE ? 2 : 4) stage3_kernel(StageArgs a)
+// TWMAX: the widest tile of the instantiation.  128: tiles of 64 or 128
+// columns, 4 CTAs per SM; 256: 256-column tiles over two 128-column blocks
+// (or one 256-column block), 4 interior warps to each halo warp, 2 CTAs per
+// SM; 512: 512-column tiles over up to four blocks, 8 interior warps to each
+// halo warp, 1 CTA per SM.
+template <bool SINGLE, int TWMAX>
+__global__ void __launch_bounds__(TWMAX / 2 + 32, TWMAX == 128 ? 4 : (TWMAX == 256 ? 2 : 1)) stage3_kernel(StageArgs a)
 {
     constexpr int NF = 3;
     constexpr int H = 4;                     // staged halo columns per side: 16 bytes of FP32
@@ -328,9 +330,10 @@ __global__ void __launch_bounds__(WIDE ? 160 : 96, WIDE ? 2 : 4) stage3_kernel(S
     static_assert(group_size<NF, 0>() + group_size<NF, 1>() + group_size<NF, 2>() == NLIVE, "ledger groups");
     // [warp][item slot] of the main piece and of a crossing tile's first piece;
     // group 0 of the first piece per thread
-    __shared__ float sLed[4][32], sLedA[4][32], sAccA[7][PIECE_MAX_THREADS];
+    constexpr int NWI = TWMAX / 64 < 4 ? 4 : TWMAX / 64;   // bank rows: interior warps
+    __shared__ float sLed[NWI][32], sLedA[NWI][32], sAccA[7][TWMAX / 2];
     const int lane = t & 31, warp = t >> 5;
-    if (t < 128) sLed[t >> 5][t & 31] = sLedA[t >> 5][t & 31] = 0.0f;
+    for (int i = t; i < NWI * 32; i += blockDim.x) sLed[i >> 5][i & 31] = sLedA[i >> 5][i & 31] = 0.0f;
     const int slot0 = group_writer_slot<NF, 0>(lane);
     float acc0[7] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};   // ledger group 0 of this pair, summed over rows
     const int slot1 = group_writer_slot<NF, 1>(lane);
@@ -662,11 +665,11 @@ __global__ void __launch_bounds__(WIDE ? 160 : 96, WIDE ? 2 : 4) stage3_kernel(S
     for (int k = warp; k < npiece; k += blockDim.x / 32) {
         const int c = k % ncol;
         if (k < ncol)
-            flush_piece<NF>(rd, brow, bcol + c, lslot, TW, sLed + c * wpc, wpc, nullptr, a.in_slot, a.base_slot,
+            flush_piece<NF>(rd, brow, bcol + c, lslot, TW, sLed + c * wpc, wpc, nullptr, 0, a.in_slot, a.base_slot,
                             a.out_slot, a.stage, a.bf);
         else
             flush_piece<NF>(rd, brow - 1, bcol + c, lslot, TW, sLedA + c * wpc, wpc,
-                            (const float (*)[PIECE_MAX_THREADS])(&sAccA[0][c * wpc * 32]), a.in_slot, a.base_slot,
+                            &sAccA[0][c * wpc * 32], TWMAX / 2, a.in_slot, a.base_slot,
                             a.out_slot, a.stage, a.bf);
     }
 }

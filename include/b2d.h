@@ -286,13 +286,13 @@ b2d_status b2d_initial_state(const b2d_config* cfg, const b2d_disk_model* model,
 /* Tile shape of the stage kernel for a context: width in zones along j (a
  * multiple of 32 dividing block_size) and height along i (dividing
  * block_size).  The paired-column FP32 kernel (precision FP32_COMP,
- * isothermal) also takes 128- or 256-column tiles that span whole blocks of
- * 64 columns or more side by side.  0 keeps the current value. */
+ * isothermal) also takes 128-, 256- or 512-column tiles that span whole
+ * blocks of 64 columns or more side by side.  0 keeps the current value. */
 b2d_status b2d_set_tile(b2d_ctx* ctx, int32_t tile_w, int32_t tile_h);
 b2d_status b2d_get_tile(const b2d_ctx* ctx, int32_t* tile_w, int32_t* tile_h);
 
 /* Row chunks of the FP32 stage kernels (the paired-column kernel: FP32_COMP,
- * isothermal, tile width 64, 128 or 256; the TMA-staged kernel: FP32 tiles
+ * isothermal, tile width 64, 128, 256 or 512; the TMA-staged kernel: FP32 tiles
  * whose width is a multiple of 32, at most 128).  rows > 0: every column strip of tile
  * width is covered in ceil(N / rows) row chunks of near-equal height (at most
  * `rows`; 8 <= rows <= block_size), each of which may cross one block
@@ -306,7 +306,7 @@ b2d_status b2d_get_strip_rows(const b2d_ctx* ctx, int32_t* rows);
 
 /* Tile autotuner: times every tile shape that divides the block size (width
  * 32..128, or 256 for FP64; height 8..128), the paired FP32 kernel's tiles
- * that span blocks (128 or 256 columns) and, where that kernel runs, the
+ * that span blocks (128, 256 or 512 columns) and, where that kernel runs, the
  * strip rows that fill one, two or three whole waves of its resident CTAs, over `reps` advances of `fold` steps with CUDA events; keeps
  * the fastest (b2d_get_tile and b2d_get_strip_rows report it).  The
  * context's state is unchanged. */

@@ -1,5 +1,5 @@
 """The paired-column FP32 kernel (isothermal, compensated FP32 state, tiles 64,
-128 or 256 wide) against the CPU oracle: every isothermal physics variant,
+128, 256 or 512 wide) against the CPU oracle: every isothermal physics variant,
 every tile width, row chunks across block rows and tiles across block
 columns, single and batched launches."""
 import dataclasses
@@ -104,6 +104,8 @@ CHUNKS = [
     ((2, 128), 256, 0),    # 256-column tiles, block-aligned rows (256 x 32)
     ((4, 64), 128, 50),    # 128-column tiles over two 64-column blocks, 6 chunks
     ((4, 64), 128, 0),
+    ((4, 128), 512, 100),  # 512-column tiles over all four block columns, 6 chunks
+    ((8, 64), 512, 40),    # 512-column tiles over eight 64-column blocks, 13 chunks
 ]
 
 
@@ -143,7 +145,8 @@ def test_row_chunks_match_block_tiles():
 
 
 @pytest.mark.parametrize("nb,bs,tiles", [(4, 64, [(64, 32, 0), (128, 32, 0), (128, 32, 50), (64, 16, 30)]),
-                                          (2, 128, [(128, 32, 0), (256, 32, 0), (256, 32, 100), (256, 64, 40)])])
+                                          (2, 128, [(128, 32, 0), (256, 32, 0), (256, 32, 100), (256, 64, 40)]),
+                                          (4, 128, [(128, 32, 0), (512, 32, 0), (512, 32, 100)])])
 def test_tiles_spanning_blocks_match(nb, bs, tiles):
     """Tiles over two block columns (and row chunks over block rows) give the
     state of block-aligned tiles bit for bit, and its ledgers to FP32
