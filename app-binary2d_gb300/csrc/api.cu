@@ -168,15 +168,15 @@ __global__ void max_speed_kernel(const RunDev* runs, int run, int slot)
 // consecutive words per warp.
 constexpr int LAYOUT_ZONES = 256;
 
-// Plane index of host-layout zone q (block-major: block, row, column).
-__device__ __forceinline__ size_t plane_index(size_t q, int N, int bs, int nb)
+// Plane index of host-layout zone q (block-major: block, row, column).  A
+// run has at most 2^31 zones (validate), so 32-bit unsigned divisions do: a
+// 64-bit division costs about 150 instructions.
+__device__ __forceinline__ size_t plane_index(unsigned q, unsigned N, unsigned bs, unsigned nb)
 {
-    const size_t r = q / bs;
-    const int lj = (int)(q - r * bs);
-    const size_t b = r / bs;
-    const int li = (int)(r - b * bs);
-    const int bi = (int)(b / nb), bj = (int)(b - (size_t)bi * nb);
-    return (size_t)(bi * bs + li) * N + (size_t)bj * bs + lj;
+    const unsigned r = q / bs, lj = q - r * bs;
+    const unsigned b = r / bs, li = r - b * bs;
+    const unsigned bi = b / nb, bj = b - bi * nb;
+    return (size_t)(bi * bs + li) * N + bj * bs + lj;
 }
 
 __global__ void __launch_bounds__(LAYOUT_ZONES) scatter_kernel(const double* src, void* dst, int N, int bs, int nb,
@@ -190,7 +190,7 @@ __global__ void __launch_bounds__(LAYOUT_ZONES) scatter_kernel(const double* src
         for (int e = t; e < nz * nf; e += LAYOUT_ZONES) buf[e] = src[q0 * nf + e];
         __syncthreads();
         if (t < nz) {
-            const size_t z = plane_index(q0 + t, N, bs, nb);
+            const size_t z = plane_index((unsigned)(q0 + t), N, bs, nb);
             for (int f = 0; f < nf; ++f) {
                 const double v = buf[t * nf + f];
                 if (store == 0) {
@@ -216,7 +216,7 @@ __global__ void __launch_bounds__(LAYOUT_ZONES) gather_kernel(const void* src, d
     for (size_t q0 = (size_t)blockIdx.x * LAYOUT_ZONES; q0 < nn; q0 += (size_t)gridDim.x * LAYOUT_ZONES) {
         const int nz = (int)min((size_t)LAYOUT_ZONES, nn - q0);
         if (t < nz) {
-            const size_t z = plane_index(q0 + t, N, bs, nb);
+            const size_t z = plane_index((unsigned)(q0 + t), N, bs, nb);
             for (int f = 0; f < nf; ++f) {
                 double v;
                 if (store == 0) v = ((const double*)src)[f * nn + z];
