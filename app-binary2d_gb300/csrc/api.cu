@@ -556,7 +556,6 @@ extern "C" b2d_ctx* b2d_create(const b2d_config* cfgs, int32_t nruns, int32_t pr
     ctx->hydro = cfgs[0].hydro_kind;
     ctx->rk = cfgs[0].rk_order;
     ctx->nf = ctx->hydro == B2D_EULER ? 4 : 3;
-    int wsize = precision == B2D_PREC_FP32_COMP ? 8 : (precision == B2D_PREC_FP64 || precision == B2D_PREC_FP32_STATE64 ? 8 : 8);
     int min_bs = 1 << 30;
     for (int i = 0; i < nruns; ++i) {
         b2d_status v = validate(cfgs[i], ctx->hydro, ctx->rk);
@@ -592,7 +591,6 @@ extern "C" b2d_ctx* b2d_create(const b2d_config* cfgs, int32_t nruns, int32_t pr
     ctx->runs.resize(nruns);
     ctx->rdev_h.resize(nruns);
     const int store = precision == B2D_PREC_FP32_COMP ? 1 : 0;
-    (void)wsize;
     for (int i = 0; i < nruns; ++i) {
         RunHost& r = ctx->runs[i];
         RunDev& d = ctx->rdev_h[i];
@@ -719,7 +717,6 @@ extern "C" b2d_status b2d_upload_state(b2d_ctx* ctx, int32_t run, const double* 
     RunHost& r = ctx->runs[run];
     size_t n = (size_t)r.N * r.N * ctx->nf;
     int store = store_of(ctx);
-    int grid = 4 * 152;
     CUDA_TRY(cudaMemcpyAsync(ctx->d_staging, cons, n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
     scatter_kernel<<<layout_blocks(r.N), LAYOUT_ZONES, 0, ctx->stream>>>(ctx->d_staging, r.slot[ctx->cur], r.N, r.bs, r.nb, ctx->nf, store);
     ctx->launches++;

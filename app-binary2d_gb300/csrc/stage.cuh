@@ -189,7 +189,7 @@ __global__ void __launch_bounds__(256) stage_kernel(StageArgs a)
     const R* xc = (const R*)(is_f64<R>() ? (const void*)rd.xc : (const void*)rd.xcf);
     const R* xv = (const R*)(is_f64<R>() ? (const void*)rd.xv : (const void*)rd.xvf);
 
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];   // one declaration for every stage kernel
     R* sP = (R*)smem_raw;                  // [4][TW+4][NF]   primitives
     R* sC = sP + 4 * (TW + 4) * NF;        // [3][TW+2][CW]   cell records
     R* sF = sC + 3 * (TW + 2) * CW;        // [2][TW+1][NF]   y-face fluxes
