@@ -102,8 +102,54 @@ def dist_env():
     return ws, rank, local
 
 
+class NvmlSampler:
+    """SM clock, its maximum and the clock-event reasons of one GPU, read from
+    NVML (libnvidia-ml, read-only queries) every `period` seconds in a
+    thread.  Raises at construction if NVML cannot be used."""
+    # nvmlClocksEventReasons bits (nvml.h): SwPowerCap, HwSlowdown, SwThermalSlowdown, HwThermalSlowdown
+    BITS = {"sw_power_cap": 0x4, "hw_slowdown": 0x8, "sw_thermal_slowdown": 0x20, "hw_thermal_slowdown": 0x40}
+
+    def __init__(self, bus_id, period=0.02):
+        lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if lib.nvmlInit_v2() != 0:
+            raise RuntimeError("nvmlInit failed")
+        self.lib, self.period = lib, period
+        self.handle = ctypes.c_void_p()
+        dom, rest = bus_id.split(":", 1)
+        for bid in ("%08x:%s" % (int(dom, 16), rest), "%04x:%s" % (int(dom, 16), rest)):
+            if lib.nvmlDeviceGetHandleByPciBusId_v2(bid.encode(), ctypes.byref(self.handle)) == 0:
+                break
+        else:
+            raise RuntimeError("no NVML handle for " + bus_id)
+        self.reasons_fn = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        mx = ctypes.c_uint()
+        if lib.nvmlDeviceGetMaxClockInfo(self.handle, 1, ctypes.byref(mx)) != 0:   # NVML_CLOCK_SM
+            raise RuntimeError("nvmlDeviceGetMaxClockInfo failed")
+        self.max_mhz = float(mx.value)
+        self.samples = []
+        self.stop = threading.Event()
+
+    def sample(self):
+        mhz, bits = ctypes.c_uint(), ctypes.c_ulonglong()
+        if self.lib.nvmlDeviceGetClockInfo(self.handle, 1, ctypes.byref(mhz)) == 0 and \
+                self.reasons_fn(self.handle, ctypes.byref(bits)) == 0:
+            self.samples.append((float(mhz.value), int(bits.value)))
+
+    def run(self):
+        while not self.stop.is_set():
+            self.sample()
+            time.sleep(self.period)
+
+    def close(self):
+        self.stop.set()
+        self.lib.nvmlShutdown()
+
+
 class Clocks:
-    """Sample nvidia-smi clocks and throttle reasons during the timed region."""
+    """Sample the SM clock and the clock-event reasons during the timed region:
+    from NVML every 20 ms where the driver library loads, else from
+    nvidia-smi every 200 ms."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
          "clocks_event_reasons.sw_power_cap")
@@ -111,9 +157,19 @@ class Clocks:
     def __init__(self, index):
         self.index = index
         self.proc = None
+        self.nvml = None
         self.lines = []
 
     def __enter__(self):
+        try:
+            import torch
+            p = torch.cuda.get_device_properties(self.index)
+            self.nvml = NvmlSampler("%x:%02x:%02x.0" % (p.pci_domain_id, p.pci_bus_id, p.pci_device_id))
+            self.t = threading.Thread(target=self.nvml.run, daemon=True)
+            self.t.start()
+            return self
+        except Exception:
+            self.nvml = None
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
                                           "--format=csv,noheader,nounits", "-lms", "200"],
@@ -129,6 +185,11 @@ class Clocks:
             self.lines.append(line.strip())
 
     def __exit__(self, *exc):
+        if self.nvml:
+            self.nvml.sample()   # at least one sample at the end of the region
+            self.nvml.stop.set()
+            self.t.join(timeout=1)
+            self.nvml.close()
         if self.proc:
             self.proc.terminate()
             try:
@@ -137,6 +198,13 @@ class Clocks:
                 self.proc.kill()
 
     def summary(self):
+        if self.nvml is not None:
+            smp = self.nvml.samples
+            if not smp:
+                return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0, "source": "nvml"}
+            reasons = sorted(n for n, b in NvmlSampler.BITS.items() if any(bits & b for _, bits in smp))
+            return {"sm_mhz": statistics.median(m for m, _ in smp), "sm_max_mhz": self.nvml.max_mhz,
+                    "reasons": reasons, "samples": len(smp), "source": "nvml, 20 ms"}
         mhz, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines:
@@ -153,7 +221,8 @@ class Clocks:
                     reasons.add(n)
         if not mhz:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
-        return {"sm_mhz": statistics.median(mhz), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(mhz)}
+        return {"sm_mhz": statistics.median(mhz), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(mhz),
+                "source": "nvidia-smi, 200 ms"}
 
 
 def cpu_sample(mesh, hydro, physics, model, seconds, nthreads):
