@@ -71,7 +71,8 @@ def link_bandwidth(torch, host_src, host_dst):
     return out
 
 
-PROFILES = {("disk_2048", "fp32_comp"): "stage3_kernel_fp32comp_disk2048.md"}
+PROFILES = {("disk_2048", "fp32_comp"): "stage3_kernel_fp32comp_disk2048.md",
+            ("euler_4096", "fp32_comp"): "stage2_kernel_fp32comp_euler4096.md"}
 
 
 def ncu_profile(workload, precision, key):
@@ -469,7 +470,8 @@ def ours(args):
                          "frac": achieved / hbm_peak, "peak_kind": peak_kind,
                          "traffic": ncu_traffic(args.workload, prec),
                          "traffic_note": ("mean DRAM bytes of the two RK2 stage launches of one step "
-                                          "(algorithmic mean 352 MB) from profiles/" + PROFILES[(args.workload, prec)])
+                                          "(algorithmic mean %.0f MB) from profiles/%s"
+                                          % (bytes_per_launch / 1e6, PROFILES.get((args.workload, prec))))
                                          if ncu_traffic(args.workload, prec) else "no ncu capture of this workload",
                          "algorithmic_bytes_per_launch": bytes_per_launch,
                          "bytes_per_zone_update": bytes_per_zone_update, "stage_ms": stage_ms,
