@@ -149,7 +149,7 @@ class NvmlSampler:
 
 class Clocks:
     """Sample the SM clock and the clock-event reasons during the timed region:
-    from NVML every 20 ms where the driver library loads, else from
+    from NVML every 20 ms where libnvidia-ml loads, else from
     nvidia-smi every 200 ms."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"

@@ -1,7 +1,7 @@
 """One-orbit accuracy of the three precisions against the CPU oracle, on the
-isothermal disk (2048², BASELINE config 2) or the Euler β-cooling disk
-(config 3, at a resolution the oracle can afford), and FP32 against FP64 on
-the GPU alone where the oracle cannot follow (config 5).
+isothermal disk of 16 x 16 blocks of 128² or the Euler β-cooling disk (at a
+resolution the oracle can afford), and FP32 against FP64 on the GPU alone
+where the oracle cannot follow (the 8192² disk).
 
 Two steps, because the oracle's orbit costs up to 8e10 zone-updates:
 
