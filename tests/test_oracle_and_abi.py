@@ -225,3 +225,30 @@ def test_oracle_reports_negative_density():
         st.advance(1, nthreads=2)
     assert e.value.err.code == 1 and e.value.err.value == -0.5
     assert (e.value.err.block_i, e.value.err.block_j, e.value.err.zone_i, e.value.err.zone_j) == (1, 1, 3, 2)
+
+
+def _run_geometry_check(tmp_path, *defines):
+    import shutil
+    import subprocess
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc):
+        pytest.skip("nvcc not available")
+    exe = str(tmp_path / "chunk_geometry_check")
+    src = os.path.join(os.path.dirname(os.path.abspath(__file__)), "chunk_geometry_check.cu")
+    subprocess.run([nvcc, "-std=c++17", "-O1", "-x", "cu", *defines, src, "-o", exe], check=True,
+                   capture_output=True, text=True)
+    return subprocess.run([exe], capture_output=True, text=True)
+
+
+def test_tile_geometry_pieces(tmp_path):
+    """Row chunks across block rows and tiles across block columns: every row
+    lies in its piece's block row, every ledger piece has one slot, and every
+    block receives exactly its count of pieces (the real runtime.cuh helpers,
+    with the stage kernels' slot formulas, on the host)."""
+    r = _run_geometry_check(tmp_path)
+    assert r.returncode == 0 and r.stdout.strip() == "ok", r.stdout
+
+
+def test_tile_geometry_check_rejects_a_wrong_slot(tmp_path):
+    r = _run_geometry_check(tmp_path, "-DPLANT_SLOT_MISTAKE")
+    assert r.returncode != 0 and "piece slot" in r.stdout, r.stdout
