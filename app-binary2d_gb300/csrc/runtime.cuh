@@ -14,7 +14,7 @@ struct df32w { float hi, lo; };
 struct RunDev {
     int N, bs, nb, nblocks;
     int tiles_i, tiles_j, ntiles, tile_base;
-    int tiles_per_block, pad_;
+    int tiles_per_block, pad_;   // partial slots per block: the most ledger pieces a block receives
     const double* xc;        // [N] cell centres by global index (block formula, mesh.rs:49-54)
     const double* xv;        // [nb][bs+1] block vertices (mesh.rs:42-47)
     const float* xcf;
@@ -25,7 +25,7 @@ struct RunDev {
     double* ledger[NSLOTS];  // [nblocks][7][nf] per slot
     double* time;            // [NSLOTS]
     long long* iter;         // [NSLOTS]
-    double* partial;         // [nblocks][tiles_per_block][7 nf]
+    double* partial;         // [nblocks][tiles_per_block][7 nf] ledger pieces of the tiles over each block
     unsigned* counter;       // [nblocks]
     double* dt;              // [1]
     double* stage_time;      // [max_stages]

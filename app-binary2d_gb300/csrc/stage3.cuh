@@ -649,7 +649,7 @@ __global__ void __launch_bounds__(TWMAX / 2 + 32, TWMAX == 128 ? 4 : (TWMAX == 2
 
     // ---- ledger pieces, one per block under the tile: its block row(s) times its
     // block column(s), each flushed by its own warp --------------------------------
-    if (interior) {   // whole warps: group 0's column sums, one warp reduction per tile
+    if (interior) {   // whole warps: group 0's column sums of the main piece's rows, one warp reduction
         float v0[8];
 #pragma unroll
         for (int m = 0; m < 7; ++m) v0[m] = acc0[m];
