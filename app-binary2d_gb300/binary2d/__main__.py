@@ -1,7 +1,7 @@
 """Command line of main.rs (src/main.rs:216-263):
 
     python -m binary2d <input.yaml|chkpt.cbor|preset> [opts.yaml|group.key=value] [...]
-           [--precision fp64|fp32_state64|fp32_comp]
+           [--precision fp64|fp32_state64|fp32_comp] [--no-autotune]
 """
 import sys
 
@@ -15,6 +15,8 @@ def main(argv=None):
         k = argv.index("--precision")
         precision = argv[k + 1]
         del argv[k:k + 2]
+    autotune = "--no-autotune" not in argv
+    argv = [a for a in argv if a != "--no-autotune"]
     print()
     print("Clemson CAL Circumbinary Disk Code (CDC) — GB300 step")
     print(_app.VERSION)
@@ -36,7 +38,7 @@ def main(argv=None):
     print("worker threads ...... GPU (%s)" % precision)
     print("grid spacing ........ %.3fa" % cfg.mesh.cell_spacing())
     print()
-    driver = _app.Driver(app, precision=precision)
+    driver = _app.Driver(app, precision=precision, autotune=autotune)
     try:
         driver.run()
     finally:

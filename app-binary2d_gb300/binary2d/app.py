@@ -384,12 +384,17 @@ def _safety(physics: Physics, crashed: bool) -> Physics:
 
 class Driver:
     """main.rs:run over a GB300 context.  `runtime_factory(physics)` builds a
-    Runtime for a Physics (tests pass a fake)."""
+    Runtime for a Physics (tests pass a fake).  With `autotune`, each context
+    times its tile shapes and row chunks once, on the first state it holds
+    (b2d_autotune leaves that state unchanged)."""
 
-    def __init__(self, app: App, precision: str = "fp64", runtime_factory=None, background=None, log=print):
+    def __init__(self, app: App, precision: str = "fp64", runtime_factory=None, background=None, log=print,
+                 autotune: bool = True):
         self.app = app
         self.precision = precision
         self.log = log
+        self.autotune = autotune
+        self._tuned = set()
         cfg = app.config
         self.background = background if background is not None else initial_state(
             cfg.mesh, cfg.hydro, cfg.physics, cfg.model)       # BlockData::from_model, main.rs:119-122
@@ -411,6 +416,9 @@ class Driver:
         rt.upload(0, s.cons, background=self.background, ledger=s.ledger, time=s.time, iteration=s.iteration)
         if s.elements is not None:
             rt.upload_elements(0, s.elements)
+        if self.autotune and id(rt) not in self._tuned and hasattr(rt, "autotune"):
+            rt.autotune()
+            self._tuned.add(id(rt))
         self._active = rt
 
     def _store(self, rt):
