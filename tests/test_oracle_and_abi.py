@@ -5,6 +5,7 @@ import math
 import os
 import re
 import subprocess
+import sys
 
 import numpy as np
 import pytest
@@ -252,3 +253,16 @@ def test_tile_geometry_pieces(tmp_path):
 def test_tile_geometry_check_rejects_a_wrong_slot(tmp_path):
     r = _run_geometry_check(tmp_path, "-DPLANT_SLOT_MISTAKE")
     assert r.returncode != 0 and "piece slot" in r.stdout, r.stdout
+
+
+def test_missing_library_fails_loudly():
+    """No CPU fallback: without libb2d.so the product path raises, and says so."""
+    code = ("import sys; sys.path.insert(0, %r)\n"
+            "from binary2d import _lib\n"
+            "try:\n"
+            "    _lib.load('/nonexistent/libb2d.so')\n"
+            "except RuntimeError as e:\n"
+            "    print('raised:', e)\n") % os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                                               "app-binary2d_gb300")
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True)
+    assert r.returncode == 0 and "raised:" in r.stdout and "no CPU fallback" in r.stdout, r.stdout + r.stderr
