@@ -385,15 +385,19 @@ def _safety(physics: Physics, crashed: bool) -> Physics:
 class Driver:
     """main.rs:run over a GB300 context.  `runtime_factory(physics)` builds a
     Runtime for a Physics (tests pass a fake).  With `autotune`, each context
-    times its tile shapes and row chunks once, on the first state it holds
-    (b2d_autotune leaves that state unchanged)."""
+    of an FP32 precision times its tile shapes and row chunks once, on the
+    first state it holds (b2d_autotune leaves that state unchanged).  The FP64
+    parity path always keeps its default tiles: its per-block ledgers are sums
+    of per-tile partials whose rounding depends on the tile shape, so a tiling
+    picked by timing would make ledgers differ from run to run and a restart
+    from a checkpoint would not continue the run bit for bit."""
 
     def __init__(self, app: App, precision: str = "fp64", runtime_factory=None, background=None, log=print,
                  autotune: bool = True):
         self.app = app
         self.precision = precision
         self.log = log
-        self.autotune = autotune
+        self.autotune = autotune and precision != "fp64"
         self._tuned = set()
         cfg = app.config
         self.background = background if background is not None else initial_state(

@@ -59,12 +59,10 @@ class Run:
     physics: Physics
 
 
-def initial_state(mesh: Mesh, hydro, physics: Physics, model: DiskModel, run: int = 0) -> np.ndarray:
-    """BlockState::from_model for the InfiniteDisk model plus the synthetic
-    cavity/noise; returns the conserved state in block layout
-    [nb, nb, bs, bs, nf]."""
-    lib = _lib.load()
-    c = to_c(mesh, hydro, physics)
+def disk_model_struct(model: DiskModel, run: int = 0) -> B2DDiskModel:
+    """The b2d_disk_model of `model` for run index `run` (plain data; building
+    it loads no library)."""
+    from .config import MODEL_KINDS
     m = B2DDiskModel()
     m.surface_density = model.surface_density
     m.mach_number = model.mach_number if model.mach_number is not None else 0.0
@@ -73,7 +71,6 @@ def initial_state(mesh: Mesh, hydro, physics: Physics, model: DiskModel, run: in
     m.noise = model.noise
     m.seed = model.seed
     m.run = run
-    from .config import MODEL_KINDS
     m.kind = MODEL_KINDS[model.kind]
     m.disk_mass = model.disk_mass
     m.disk_width = model.disk_width
@@ -81,8 +78,22 @@ def initial_state(mesh: Mesh, hydro, physics: Physics, model: DiskModel, run: in
     m.disk_softening = model.softening_length
     m.core_radius = model.core_radius
     m.edge_width = model.edge_width
-    nf = num_fields(hydro)
-    out = np.empty((mesh.num_blocks, mesh.num_blocks, mesh.block_size, mesh.block_size, nf), dtype=np.float64)
+    return m
+
+
+def state_shape(mesh: Mesh, hydro) -> Tuple[int, ...]:
+    """Block layout [nb, nb, bs, bs, nf] of a run's conserved state."""
+    return (mesh.num_blocks, mesh.num_blocks, mesh.block_size, mesh.block_size, num_fields(hydro))
+
+
+def initial_state(mesh: Mesh, hydro, physics: Physics, model: DiskModel, run: int = 0) -> np.ndarray:
+    """BlockState::from_model for the InfiniteDisk model plus the synthetic
+    cavity/noise; returns the conserved state in block layout
+    [nb, nb, bs, bs, nf]."""
+    lib = _lib.load()
+    c = to_c(mesh, hydro, physics)
+    m = disk_model_struct(model, run)
+    out = np.empty(state_shape(mesh, hydro), dtype=np.float64)
     _check(lib.b2d_initial_state(ctypes.byref(c), ctypes.byref(m), _dp(out)))
     return out
 

@@ -1693,9 +1693,8 @@ extern "C" b2d_status b2d_autotune(b2d_ctx* ctx, int32_t fold, int32_t reps, int
 // One RK stage that allocates nothing.
 //
 // Some callers cannot call cudaMalloc: a host code that owns a fixed device
-// memory pool and forbids allocation by libraries, an allocator-less embedded
-// runtime, or code that runs while another framework is capturing the stream
-// into a graph and allocation would break it.  They hand over every input and
+// memory pool and forbids allocation by libraries, or an allocator-less
+// embedded runtime.  They hand over every input and
 // output buffer themselves; the scratch the stage kernel needs (its run
 // descriptor, the binary at the stage time, per-tile ledger partials, block
 // counters, the max-speed word and the failure key) lives in the file-scope
@@ -1754,6 +1753,11 @@ extern "C" b2d_status b2d_stage_noalloc(const b2d_config* cfg, const double* d_i
     const int bs = cfg->block_size, nb = cfg->num_blocks, N = bs * nb, nblocks = nb * nb;
     int tw = default_tile_w(bs), th = std::min(64, bs);
     while (bs % th) th /= 2;
+    // one thread per tile column: a block width that is not a multiple of 32
+    // is its own tile, which the FP64 kernel's 256-thread bound must hold
+    if (tw > 256)
+        return fail(B2D_ERR_INVALID, "b2d_stage_noalloc: block_size " + std::to_string(bs) +
+                                         " must be a multiple of 32 or at most 256");
     const int tiles_per_block = (bs / th) * (bs / tw);
     const int ntiles = (N / th) * (N / tw);
 

@@ -14,14 +14,10 @@ static cudaError_t launch_two_impl(const StageArgs& a, int grid, int tw, cudaStr
 {
     auto k = stage2_kernel<NF, STORE, SINGLE>;
     size_t smem = s2_smem_bytes(NF, STORE, tw);
-    static size_t configured = 0;
     // opt in for every size: the kernel's static shared memory counts toward
     // the 48 KB that needs no opt-in
-    if (smem > configured) {
-        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        configured = smem;
-    }
+    cudaError_t e = opt_in_smem((const void*)k, smem);
+    if (e != cudaSuccess) return e;
     k<<<grid, tw + 32, smem, s>>>(a);
     return cudaGetLastError();
 }
@@ -38,12 +34,8 @@ static cudaError_t launch_three_impl(const StageArgs& a, int grid, int tw, cudaS
 {
     auto k = stage3_kernel<SINGLE, TWMAX>;
     size_t smem = s3_smem_bytes(tw);
-    static size_t configured = 0;
-    if (smem > configured) {
-        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        configured = smem;
-    }
+    cudaError_t e = opt_in_smem((const void*)k, smem);
+    if (e != cudaSuccess) return e;
     k<<<grid, tw / 2 + 32, smem, s>>>(a);
     return cudaGetLastError();
 }
@@ -72,7 +64,7 @@ int stage_ctas_per_sm(int nf, int store, int nruns, int tw)
         else if (tw == 256) k = nruns == 1 ? stage3_kernel<true, 256> : stage3_kernel<false, 256>;
         else k = nruns == 1 ? stage3_kernel<true, 512> : stage3_kernel<false, 512>;
         // the opt-in above 48 KB of dynamic shared memory, as at launch
-        if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
+        if (opt_in_smem((const void*)k, smem) != cudaSuccess) return 0;
         cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, tw / 2 + 32, smem);
         return e == cudaSuccess ? n : 0;
     }

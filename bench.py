@@ -11,8 +11,8 @@ plus background exceed the 129 MB L2, so no flush is needed between steps.
 Arms:
   --impl ours (default)  the CUDA path through the C ABI (libb2d.so)
   --impl reference       the reference's CPU algorithm restated in C (the
-                         oracle port), all host threads, one RK step of the
-                         same mesh per bench step
+                         oracle port), all host threads, one advance of
+                         fold 10 RK2 steps of the same mesh per bench step
 
 Under torchrun (N > 1) every rank advances its own disk (independent runs,
 weak scaling, no collective in the data path); timing is the max over ranks.
@@ -38,6 +38,7 @@ import numpy as np
 METRIC = "zone-updates/s: mixed-prec+batched vs plain FP64 on 1 GB300 at stated L1 err; %HBM"
 UNIT = "zone-updates/s"
 FOLD = 10
+WORKLOAD_2048 = "iso disk 2048^2 (16x16 blocks of 128^2), q=1 e=0 Mach 10, RK2, fold 10"
 
 
 def peaks():
@@ -227,49 +228,54 @@ class Clocks:
 
 
 def cpu_sample(mesh, hydro, physics, model, seconds, nthreads):
-    """The oracle port on the host cores: RK steps of the same mesh for about
-    `seconds`; returns zone-updates/s."""
-    import binary2d as b2
+    """The oracle port on the host cores: advances of FOLD RK steps of the same
+    mesh for about `seconds`; returns (zone-updates/s, RK steps).  The state
+    comes from the oracle's own initial model, so this leg loads no product
+    library."""
     from oracle import binding
-    cons = b2.initial_state(mesh, hydro, physics, model)
-    st = binding.OracleState(b2.to_c(mesh, hydro, physics), cons)
-    st.advance(1, nthreads=nthreads)  # warm
+    cons, cfg = binding.disk_initial_state(mesh, hydro, physics, model)
+    st = binding.OracleState(cfg, cons)
+    st.advance(FOLD, nthreads=nthreads)  # warm
     n, t0 = 0, time.perf_counter()
     while True:
-        st.advance(1, nthreads=nthreads)
+        st.advance(FOLD, nthreads=nthreads)
         n += 1
         el = time.perf_counter() - t0
         if el >= seconds and n >= 2:
             break
-    return mesh.total_zones() * n / el, n
+    return mesh.total_zones() * FOLD * n / el, FOLD * n
 
 
 def reference_arm(args):
+    """The reference's algorithm on the host cores (the oracle port, C, FP64,
+    one pool task per block and phase like the reference's tokio design,
+    2 x cores threads as src/app.rs:125-131 defaults), on the GPU arm's
+    workload and cadence: one bench step is one advance of FOLD RK2 steps of
+    the 2048^2 disk (setups/iso-circular.yaml:31).  Loads only the oracle."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return 0
-    import binary2d as b2
-    mesh, hydro, physics, model = b2.presets.disk_2048(seed=1)
-    nthreads = 2 * (os.cpu_count() or 1)   # the reference's default, src/app.rs:125-131
+    from binary2d import presets
     from oracle import binding
-    cons = b2.initial_state(mesh, hydro, physics, model)
-    st = binding.OracleState(b2.to_c(mesh, hydro, physics), cons)
+    mesh, hydro, physics, model = presets.disk_2048(seed=1)
+    nthreads = 2 * (os.cpu_count() or 1)   # the reference's default, src/app.rs:125-131
+    cons, cfg = binding.disk_initial_state(mesh, hydro, physics, model)
+    st = binding.OracleState(cfg, cons)
     for _ in range(args.warmup):
-        st.advance(1, nthreads=nthreads)
+        st.advance(FOLD, nthreads=nthreads)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        st.advance(1, nthreads=nthreads)
+        st.advance(FOLD, nthreads=nthreads)
     el = time.perf_counter() - t0
-    v = mesh.total_zones() * args.steps / el
+    v = mesh.total_zones() * FOLD * args.steps / el
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "iso disk 2048^2 (16x16 blocks of 128^2), one RK2 step per bench step",
-                   "global_batch": 1, "parallelism": "host threads"},
+        "config": {"workload": WORKLOAD_2048, "global_batch": 1, "parallelism": "host threads"},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": nthreads, "kind": "port",
-                         "sample": "%d RK2 steps of the 2048^2 disk, %d threads on %d host cores"
-                                   % (args.steps, nthreads, os.cpu_count() or 1)},
+                         "sample": "%d advances of %d RK2 steps of the 2048^2 disk, %d threads on %d host cores"
+                                   % (args.steps, FOLD, nthreads, os.cpu_count() or 1)},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -295,7 +301,7 @@ def ours(args):
         return sweep_bench(args, torch, b2, ws, rank, dist)
     if args.workload == "disk_2048":
         mesh, hydro, physics, model = b2.presets.disk_2048(seed=1 + rank)
-        wname = "iso disk 2048^2 (16x16 blocks of 128^2), q=1 e=0 Mach 10, RK2, fold 10"
+        wname = WORKLOAD_2048
     elif args.workload == "disk_512":
         mesh, hydro, physics, model = b2.presets.disk_512(seed=1 + rank)
         wname = "iso disk 512^2 (8x8 blocks of 64^2), q=1 e=0 Mach 10, RK2, fold 10"
@@ -448,8 +454,8 @@ def ours(args):
         nthreads = 2 * (os.cpu_count() or 1)
         v, n = cpu_sample(mesh, hydro, physics, model, args.cpu_seconds, nthreads)
         cpu = {"value": v, "unit": UNIT, "cores": nthreads, "kind": "port",
-               "sample": "%d RK2 steps of the same %d^2 mesh with the C oracle, %d threads on %d host cores"
-                         % (n, mesh.zones_per_side(), nthreads, os.cpu_count() or 1)}
+               "sample": "%d RK2 steps (advances of %d) of the same %d^2 mesh with the C oracle, %d threads on %d host cores"
+                         % (n, FOLD, mesh.zones_per_side(), nthreads, os.cpu_count() or 1)}
 
     if rank == 0:
         line = {

@@ -347,8 +347,8 @@ b2d_status b2d_set_device(int32_t device);
 /* ------------------------------------------------------------------------ */
 /* One RK stage that allocates nothing.  No counterpart in the reference: it
  * serves callers that cannot call cudaMalloc — a host code that owns a fixed
- * device memory pool and forbids allocation by libraries, an allocator-less
- * runtime, or code running while another framework captures the stream.
+ * device memory pool and forbids allocation by libraries, or an
+ * allocator-less runtime.
  *
  * Performs one try_advance_rk stage with the FP64 kernel on caller-owned
  * device buffers: state planes [nf][N][N] (N = num_blocks · block_size,
@@ -362,7 +362,8 @@ b2d_status b2d_set_device(int32_t device);
  *
  * Its scratch is one file-scope __device__ array of 4 MiB that every GPU that
  * loads the library holds until exit; meshes whose tile partials and
- * geometry tables do not fit are rejected with B2D_ERR_INVALID.  The first
+ * geometry tables do not fit, and block sizes that are neither a multiple of
+ * 32 nor at most 256, are rejected with B2D_ERR_INVALID.  The first
  * call on a device looks up the array's device address (cudaGetSymbolAddress)
  * and should come before any stream capture.  All calls share the array:
  * calls that overlap on the GPU (other streams, other host threads) race.

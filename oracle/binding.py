@@ -117,6 +117,17 @@ def initial_state(cfg, model_struct, shape):
     return out
 
 
+def disk_initial_state(mesh, hydro, physics, model, run=0):
+    """The oracle's initial state of a run described by the host package's
+    Mesh / hydro / Physics / DiskModel (BlockState::from_model,
+    src/state.rs:74-86, plus the synthetic cavity and noise), without loading
+    the product library.  Returns (state in block layout, oracle config)."""
+    from binary2d.config import to_c
+    from binary2d.scheme import disk_model_struct, state_shape
+    cfg = to_c(mesh, hydro, physics)
+    return initial_state(cfg, disk_model_struct(model, run), state_shape(mesh, hydro)), cfg
+
+
 def max_signal_speed(cfg, cons):
     cons = np.ascontiguousarray(cons, np.float64)
     return load().oracle_max_signal_speed(ctypes.byref(cfg), _dp(cons))

@@ -198,15 +198,16 @@ def test_checkpoint_restart_is_bitwise_continuous(tmp_path):
     d = yaml_lite.loads(CONFIG)
     d["control"].update(num_orbits=0.004, output_directory=str(tmp_path / "a"), fallback_stack_size=0)
     cfg = app.config_from_dict(d)
-    # one tiling for both drivers: the ledgers' per-tile partial sums round
-    # differently under different tile shapes (the states do not)
-    whole = app.Driver(app.App.from_config(cfg), log=lambda *_: None, autotune=False)
+    # default driver settings: the FP64 path keeps its default tiles (the
+    # ledgers' per-tile partial sums round differently under different tile
+    # shapes), so no autotune runs here
+    whole = app.Driver(app.App.from_config(cfg), log=lambda *_: None)
     full = whole.run()
     whole.close()
     # restart from the first checkpoint and run to the same end time
     first = app.read_checkpoint(str(tmp_path / "a" / "chkpt.0000.cbor"))
     first.config.control.output_directory = str(tmp_path / "b")
-    again = app.Driver(first, log=lambda *_: None, autotune=False)
+    again = app.Driver(first, log=lambda *_: None)
     rest = again.run()
     again.close()
     assert rest.state.iteration == full.state.iteration
@@ -218,14 +219,21 @@ def test_checkpoint_restart_is_bitwise_continuous(tmp_path):
 
 @pytest.mark.gpu
 def test_driver_autotune_keeps_the_run(tmp_path):
-    """The driver's one autotune per context (trial advances on the loaded
-    state, then discarded) leaves the run itself unchanged: the same state bit
-    for bit, and the same ledgers up to the summation order of the tiles."""
+    """The driver's one autotune per FP32 context (trial advances on the
+    loaded state, then discarded) leaves the run itself unchanged: the same
+    state bit for bit, and the same ledgers up to the FP32 summation order of
+    the tiles.  The FP64 driver does not autotune."""
+    d = yaml_lite.loads(CONFIG)
+    assert app.Driver(app.App.from_config(app.config_from_dict(d)), log=lambda *_: None,
+                      runtime_factory=lambda p: None).autotune is False
     out = []
     for tune in (False, True):
         d = yaml_lite.loads(CONFIG)
         d["control"].update(num_orbits=0.004, output_directory=str(tmp_path / str(tune)), fallback_stack_size=0)
-        drv = app.Driver(app.App.from_config(app.config_from_dict(d)), log=lambda *_: None, autotune=tune)
+        d["mesh"]["block_size"] = 64      # 64-column blocks: the paired FP32 kernel's tiles are candidates
+        drv = app.Driver(app.App.from_config(app.config_from_dict(d)), precision="fp32_comp",
+                         log=lambda *_: None, autotune=tune)
+        assert drv.autotune is tune
         res = drv.run()
         drv.close()
         out.append(res.state)
@@ -233,4 +241,4 @@ def test_driver_autotune_keeps_the_run(tmp_path):
     assert a.iteration == b.iteration and a.time == b.time
     assert np.array_equal(a.cons, b.cons)
     scale = np.maximum(np.abs(a.ledger).sum(axis=(0, 1)), 1e-300)
-    assert (np.abs(a.ledger - b.ledger).sum(axis=(0, 1)) / scale).max() <= 1e-12
+    assert (np.abs(a.ledger - b.ledger).sum(axis=(0, 1)) / scale).max() <= 1e-5

@@ -37,3 +37,15 @@ def test_reference_arm_other_ranks_exit_without_work():
     r = _bench({"WORLD_SIZE": "2", "RANK": "1", "LOCAL_RANK": "1"}, "--steps", "1", "--warmup", "0")
     assert r.returncode == 0, r.stderr[-2000:]
     assert not [ln for ln in r.stdout.splitlines() if ln.startswith("{")], r.stdout
+
+
+def test_reference_arm_loads_no_product_library():
+    """The reference arm builds its state with the oracle's initial model and
+    advances the oracle only: libb2d.so is never mapped into the process."""
+    code = ("import sys; sys.argv = ['bench.py', '--impl', 'reference', '--steps', '1', '--warmup', '0']\n"
+            "import bench; bench.main()\n"
+            "maps = open('/proc/self/maps').read()\n"
+            "print('LIBB2D' if 'libb2d' in maps else 'CLEAN', 'ORACLE' if 'liboracle' in maps else 'NO-ORACLE')\n")
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert r.stdout.strip().splitlines()[-1] == "CLEAN ORACLE", r.stdout
