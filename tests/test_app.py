@@ -241,4 +241,6 @@ def test_driver_autotune_keeps_the_run(tmp_path):
     assert a.iteration == b.iteration and a.time == b.time
     assert np.array_equal(a.cons, b.cons)
     scale = np.maximum(np.abs(a.ledger).sum(axis=(0, 1)), 1e-300)
-    assert (np.abs(a.ledger - b.ledger).sum(axis=(0, 1)) / scale).max() <= 1e-5
+    # per-tile FP32 partial sums in another order: the FP32 ledger tolerance
+    # of the parity tests
+    assert (np.abs(a.ledger - b.ledger).sum(axis=(0, 1)) / scale).max() <= 1e-4
