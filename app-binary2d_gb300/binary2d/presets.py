@@ -55,12 +55,16 @@ def euler_beta_disk(num_blocks: int = 32, block_size: int = 128, seed: int = 3):
     hydro = Euler(gamma_law_index=5.0 / 3.0, cooling_coefficient=0.0, cooling_beta=10.0,
                   pressure_floor=1e-8, density_floor=1e-6)
     # what the workload leaves open follows the reference's cooling-cbd setup
-    # (setups/cooling-cbd.yaml): sink rate 1, buffer scale 1, CFL 0.3, PLM 1.8.
-    # (With the isothermal presets' sink rate 10 the binary swallows more than
-    # its own mass in a third of an orbit at 4096^2, and one block's accretion
-    # in one stage unbinds the perturbed orbit: OrbitalEvolutionError.)
+    # (setups/cooling-cbd.yaml): sink rate 1, buffer scale 1, PLM 1.8; and CFL
+    # 0.1.  At 4096^2 the flow between the bodies develops a density spike
+    # that the scheme does not hold at larger steps: with CFL 0.3 the state
+    # turns NaN near the centre at t = 3.16 (the reference's density floor
+    # passes NaN, so the run stops only when the orbital-element ledger meets
+    # it: OrbitalEvolutionError), with 0.2 at t = 5.65 and with 0.15 at
+    # t = 6.26; fold, PLM, softening, sink rate and the Mach ceiling do not
+    # move it.  The 512^2 disk completes an orbit at any of these.
     physics = Physics(buffer_rate=1000.0, buffer_scale=1.0, binary_eccentricity=0.5, binary_mass_ratio=0.5,
-                      cfl=0.3, plm=1.8, rk_order="RK2", sink_radius=0.05, sink_rate=1.0,
+                      cfl=0.1, plm=1.8, rk_order="RK2", sink_radius=0.05, sink_rate=1.0,
                       viscosity=("alpha", 0.1), softening_length=0.05)
     # Σ = 1 everywhere (no cavity), as the workload is described.  Two additions
     # keep it finite at 4096^2 (the oracle blows up within 4 steps without them):

@@ -17,6 +17,11 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libb2d.so")
+# The read-set check build (B2D_POISON, see csrc/tma.cuh): the same library
+# with never-written shared-memory slots and unused guard values set to NaN.
+# Tests load it to show that the states do not change; it is built on demand.
+POISON_BUILD = os.path.join(HERE, "_build_poison")
+POISON_LIB = os.path.join(POISON_BUILD, "libb2d.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -55,23 +60,27 @@ def _compile(cmd):
     return r.stdout
 
 
-def build(force: bool = False, verbose: bool = False) -> str:
+def build(force: bool = False, verbose: bool = False, poison: bool = False) -> str:
+    """Compile libb2d.so (poison=True: the read-set check variant in
+    _build_poison/) if a source is newer than it; returns its path."""
+    build_dir, lib = (POISON_BUILD, POISON_LIB) if poison else (BUILD, LIB)
+    extra = ["-DB2D_POISON"] if poison else []
     deps = _sources() + [os.path.abspath(__file__)]
-    if not force and not _stale(LIB, deps):
-        return LIB
-    os.makedirs(BUILD, exist_ok=True)
+    if not force and not _stale(lib, deps):
+        return lib
+    os.makedirs(build_dir, exist_ok=True)
     nvcc = _nvcc()
     jobs = []
     objs = []
     for src, flags in UNITS.items():
-        obj = os.path.join(BUILD, src + ".o")
+        obj = os.path.join(build_dir, src + ".o")
         objs.append(obj)
-        cmd = [nvcc] + ARCH + NVCC_COMMON + flags + ["-c", os.path.join(CSRC, src), "-o", obj]
+        cmd = [nvcc] + ARCH + NVCC_COMMON + flags + extra + ["-c", os.path.join(CSRC, src), "-o", obj]
         if verbose:
             cmd += ["-Xptxas", "-v"]
         jobs.append(cmd)
     for src, flags in HOST_UNITS.items():
-        obj = os.path.join(BUILD, src + ".o")
+        obj = os.path.join(build_dir, src + ".o")
         objs.append(obj)
         jobs.append(["g++"] + flags + ["-I", INCLUDE, "-c", os.path.join(CSRC, src), "-o", obj])
     with cf.ThreadPoolExecutor(max_workers=len(jobs)) as ex:
@@ -79,10 +88,10 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if verbose:
         for o in outs:
             print(o)
-    tmp = LIB + ".tmp%d" % os.getpid()
+    tmp = lib + ".tmp%d" % os.getpid()
     _compile([nvcc] + ARCH + ["-shared", "-Xcompiler", "-fPIC", "-o", tmp] + objs + ["-lpthread"])
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":

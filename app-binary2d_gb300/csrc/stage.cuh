@@ -19,6 +19,7 @@
 
 #include "physics.cuh"
 #include "runtime.cuh"
+#include "tma.cuh"
 
 namespace b2d {
 
@@ -193,6 +194,7 @@ __global__ void __launch_bounds__(256) stage_kernel(StageArgs a)
     R* sP = (R*)smem_raw;                  // [4][TW+4][NF]   primitives
     R* sC = sP + 4 * (TW + 4) * NF;        // [3][TW+2][CW]   cell records
     R* sF = sC + 3 * (TW + 2) * CW;        // [2][TW+1][NF]   y-face fluxes
+    poison_dynamic_smem(smem_raw);
     __syncthreads();
 
     const R theta = R(P.plm), pdt = R(P.pdt);

@@ -458,6 +458,7 @@ __global__ void __launch_bounds__(160, (NF == 3 && STORE == 1) ? 4 : 3) stage2_k
         }
     };
 
+    poison_dynamic_smem(smem_raw);
     if (producer) {
         for (int s = 0; s < S2_SLOTS + S2_USLOTS; ++s) mbar_init(bars + s, 1);
         fence_mbar_init();

@@ -299,6 +299,7 @@ __global__ void __launch_bounds__(TWMAX / 2 + 32, TWMAX == 128 ? 4 : (TWMAX == 2
         }
     };
 
+    poison_dynamic_smem(smem_raw);
     if (producer) {
         for (int s = 0; s < S3_SLOTS + S3_USLOTS; ++s) mbar_init(bars + s, 1);
         fence_mbar_init();
@@ -387,7 +388,13 @@ __global__ void __launch_bounds__(TWMAX / 2 + 32, TWMAX == 128 ? 4 : (TWMAX == 2
             const float4* prow = sP + (rg & 1) * (TW + 4);
             const float4 l4 = prow[HR + p];                    // column c0 - 1 (in the row, unused, for the -2 pair)
             const float4 r4 = prow[p + 2];                     // column c0 + 2 (in the row, unused, for the TW pair)
-            const float lv[3] = {l4.x, l4.y, l4.z}, rv[3] = {r4.x, r4.y, r4.z};
+            float lv[3] = {l4.x, l4.y, l4.z}, rv[3] = {r4.x, r4.y, r4.z};
+            // the two stencil points outside the staged columns: NaN in a
+            // read-set check build (tma.cuh), whose states must not change
+            if (hl == 0)
+                for (int f = 0; f < 3; ++f) lv[f] = poison_or(lv[f]);
+            if (hl == 1)
+                for (int f = 0; f < 3; ++f) rv[f] = poison_or(rv[f]);
             const float2 thx = make_float2((Pm1[0].x < pdt || P0[0].x < pdt || pn[0].x < pdt) ? 0.0f : theta,
                                            (Pm1[0].y < pdt || P0[0].y < pdt || pn[0].y < pdt) ? 0.0f : theta);
             const float2 thy = make_float2((lv[0] < pdt || P0[0].x < pdt || P0[0].y < pdt) ? 0.0f : theta,
@@ -413,6 +420,12 @@ __global__ void __launch_bounds__(TWMAX / 2 + 32, TWMAX == 128 ? 4 : (TWMAX == 2
             sR0[o + HR] = make_float4(P0[0].y, P0[1].y, P0[2].y, gy[0].y);
             sR1[o + HR] = make_float4(gy[1].y, gy[2].y, tyy.y, txy.y);
             sR2[o + HR] = make_float4(gx[0].y, gx[1].y, gx[2].y, txx.y);
+#ifdef B2D_POISON
+            // the records of the outer guard columns -2 and TW + 1, which no face reads
+            const float4 nan4 = make_float4(poison_or(0.0f), poison_or(0.0f), poison_or(0.0f), poison_or(0.0f));
+            if (hl == 0) sR0[o] = sR1[o] = sR2[o] = nan4;
+            if (hl == 1) sR0[o + HR] = sR1[o + HR] = sR2[o + HR] = nan4;
+#endif
 #pragma unroll
             for (int f = 0; f < NF; ++f) xg[f] = gx[f];
             xtn = txx;
@@ -449,6 +462,9 @@ __global__ void __launch_bounds__(TWMAX / 2 + 32, TWMAX == 128 ? 4 : (TWMAX == 2
                 float4* fo = sF + (rq & 1) * (TW + 2) + p;
                 fo[0] = make_float4(F[0].x, F[1].x, F[2].x, 0.0f);
                 fo[HF] = make_float4(F[0].y, F[1].y, F[2].y, 0.0f);
+#ifdef B2D_POISON
+                if (hl == 1) fo[HF] = make_float4(poison_or(0.0f), poison_or(0.0f), poison_or(0.0f), 0.0f);  // face TW + 1
+#endif
             }
         };
         float2 fxn[NF];

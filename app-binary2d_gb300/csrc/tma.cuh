@@ -68,4 +68,35 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t b
                  : "memory");
 }
 
+// Read-set check.  A build with B2D_POISON defined fills every stage kernel's
+// dynamic shared memory with quiet NaN before the kernel uses it (each 32-bit
+// word, so an FP64 slot reads as NaN too), and the paired kernel also sets the
+// stencil points its halo lanes read from outside the staged columns to NaN.
+// A slot that a zone's update reads without the kernel having written it, or
+// a guard-column value that reaches a zone's update, then turns that zone NaN;
+// a poisoned build that reproduces the normal build's states bit for bit shows
+// that neither happens.  Without B2D_POISON this is empty.
+__device__ __forceinline__ void poison_dynamic_smem(unsigned char* base)
+{
+#ifdef B2D_POISON
+    uint32_t bytes;
+    asm volatile("mov.u32 %0, %%dynamic_smem_size;" : "=r"(bytes));
+    for (uint32_t i = 4 * threadIdx.x; i + 4 <= bytes; i += 4 * blockDim.x)
+        *(uint32_t*)(base + i) = 0x7fc00000u;
+    __syncthreads();
+#else
+    (void)base;
+#endif
+}
+
+__device__ __forceinline__ float poison_or(float v)
+{
+#ifdef B2D_POISON
+    (void)v;
+    return __int_as_float(0x7fc00000);
+#else
+    return v;
+#endif
+}
+
 }  // namespace b2d

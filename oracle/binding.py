@@ -42,6 +42,11 @@ def load():
                                        c_int32, ctypes.POINTER(OracleError), c_dp, ctypes.c_int64, c_dp]
         lib.oracle_max_signal_speed.restype = c_double
         lib.oracle_max_signal_speed.argtypes = [vp, c_dp]
+        lib.oracle_max_signal_speed_rows.restype = c_double
+        lib.oracle_max_signal_speed_rows.argtypes = [vp, c_dp, c_int32, c_int32]
+        lib.oracle_stage_rows.restype = c_int32
+        lib.oracle_stage_rows.argtypes = [vp, c_dp, c_dp, c_dp, c_double, c_dp, c_dp, c_dp, c_dp, c_double,
+                                          c_double, c_int32, c_int32, ctypes.POINTER(OracleError)]
         lib.oracle_initial_state.restype = c_int32
         lib.oracle_initial_state.argtypes = [vp, vp, c_dp]
         lib.oracle_orbital_state.restype = None
@@ -131,6 +136,26 @@ def disk_initial_state(mesh, hydro, physics, model, run=0):
 def max_signal_speed(cfg, cons):
     cons = np.ascontiguousarray(cons, np.float64)
     return load().oracle_max_signal_speed(ctypes.byref(cfg), _dp(cons))
+
+
+def max_signal_speed_rows(cfg, cons, row_lo, row_hi):
+    """The maximum signal speed over block rows [row_lo, row_hi) of cons."""
+    return load().oracle_max_signal_speed_rows(ctypes.byref(cfg), _dp(cons), int(row_lo), int(row_hi))
+
+
+def stage_rows(cfg, cons_in, cons_out, background, led_in, led_out, time, dt, row_lo, row_hi,
+               base=None, led_base=None, bf=0.0):
+    """One RK stage of the blocks in block rows [row_lo, row_hi) (a row slab):
+    reads the slab and its 2-zone halo rows of cons_in, writes the slab of
+    cons_out and led_out; with `base` the RK average with weight bf follows.
+    Raises OracleHydroError on a failing zone of the slab."""
+    err = OracleError()
+    rc = load().oracle_stage_rows(ctypes.byref(cfg), _dp(cons_in), _dp(cons_out),
+                                  None if base is None else _dp(base), float(bf), _dp(background), _dp(led_in),
+                                  _dp(led_out), None if led_base is None else _dp(led_base), float(time), float(dt),
+                                  int(row_lo), int(row_hi), ctypes.byref(err))
+    if rc:
+        raise OracleHydroError(err)
 
 
 def orbital_state(cfg, t):

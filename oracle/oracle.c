@@ -1014,6 +1014,19 @@ double oracle_max_signal_speed(const oracle_config* c, const double* cons)
     return a;
 }
 
+/* State::max_signal_speed (state.rs:121-133) over the blocks of block rows
+ * [row_lo, row_hi) of a whole-mesh array: a row slab's share of the global
+ * maximum, which the slabs' owners reduce with max. */
+double oracle_max_signal_speed_rows(const oracle_config* c, const double* cons, int32_t row_lo, int32_t row_hi)
+{
+    int nf = nfields(c), nb = c->num_blocks, bs = c->block_size;
+    size_t per_row = (size_t)nb * bs * bs;
+    double a = 0.0;
+    for (size_t z = (size_t)row_lo * per_row; z < (size_t)row_hi * per_row; ++z)
+        a = fmax(zone_max_signal_speed(c, cons + z * nf), a);
+    return a;
+}
+
 int oracle_advance(const oracle_config* c, double* cons, double* ledger, const double* background,
                    double* time, int64_t* iteration, int32_t fold, double* dt_out,
                    int32_t nthreads, oracle_error* err, double* tracers, int64_t ntracers,
@@ -1145,6 +1158,115 @@ int oracle_advance(const oracle_config* c, double* cons, double* ledger, const d
     for (int k = 0; k < 4; ++k) { free(st[k].cons); free(st[k].led); free(st[k].tr); free(st[k].el); }
     for (int t = 0; t < nthreads; ++t) free(s->scratch[t]);
     free(s->scratch);
+    free(s->xc); free(s->xv); free(s->prim); free(s->perr); free(s->pbad); free(s->pzone); free(s->unbound);
+    free(s->fxs); free(s->fys);
+    return rc;
+}
+
+/* One RK stage (try_advance_rk, scheme.rs:88-173) of the blocks in block
+ * rows [row_lo, row_hi) only: the unit of work of a split of the mesh into
+ * row slabs, one per rank (no counterpart in the reference, which advances
+ * every block in one process).  The arrays are whole-mesh, block layout; of
+ * cons_in the stage reads the slab and its halo rows, the 2 zone rows on
+ * either side that the halo extension takes from the neighbouring block rows
+ * (extend_from_neighbor_arrays_2d with 2 guard zones, scheme.rs:126-127;
+ * periodic neighbours, mesh.rs:101-110), so a rank that holds its slab and
+ * the neighbours' edge rows computes its blocks exactly as a whole-mesh
+ * stage does.  (The primitives of the neighbouring block rows are converted
+ * whole, but only their halo rows are read, and a failure is reported for
+ * the slab's own blocks: a neighbour's failure is its owner's to report.)
+ * With base_cons the weighted average out = out (1 - bf) + base bf follows,
+ * for the state and the ledger (state.rs:183-199).  Single-threaded; the
+ * orbital-element change is not tracked.  Returns 0 or the error code of the
+ * slab's first failing block in block order. */
+int oracle_stage_rows(const oracle_config* c, const double* cons_in, double* cons_out, const double* base_cons,
+                      double bf, const double* background, const double* led_in, double* led_out,
+                      const double* led_base, double time, double dt, int32_t row_lo, int32_t row_hi,
+                      oracle_error* err)
+{
+    int nf = nfields(c), nb = c->num_blocks, bs = c->block_size;
+    int nblocks = nb * nb, n = bs * bs;
+    if (row_lo < 0 || row_hi > nb || row_lo >= row_hi) return -1;
+    size_t ncons = (size_t)nblocks * n * nf;
+    advance_ctx a;
+    memset(&a, 0, sizeof a);
+    stage_ctx* s = &a.st;
+    s->c = c;
+    s->nf = nf;
+    s->nb = nb;
+    s->bs = bs;
+    s->dx = cell_spacing(c);
+    s->dt = dt;
+    s->time = time;
+    s->bg = background;
+    orbital_state_from_time(c, time, &s->o);
+    s->cons_in = cons_in;
+    s->cons_out = cons_out;
+    s->led_in = led_in;
+    s->led_out = led_out;
+    s->xc = malloc(sizeof(double) * nb * bs);
+    s->xv = malloc(sizeof(double) * nb * (bs + 1));
+    for (int b = 0; b < nb; ++b) {
+        oracle_cell_centers(c, b, s->xc + b * bs);
+        oracle_block_vertices(c, b, s->xv + b * (bs + 1));
+    }
+    s->prim = malloc(sizeof(double) * ncons);
+    s->perr = calloc(nblocks, sizeof(int));
+    s->pbad = calloc(nblocks, sizeof(double));
+    s->pzone = calloc(nblocks, sizeof(int));
+    s->unbound = calloc(nblocks, sizeof(int));
+    s->fxs = malloc(sizeof(double) * (size_t)nblocks * (bs + 1) * bs * nf);
+    s->fys = malloc(sizeof(double) * (size_t)nblocks * (bs + 1) * bs * nf);
+    size_t E = bs + 4;
+    double* scratch = malloc(sizeof(double) * (E * E + 2 * (bs + 2) * E) * nf);
+    s->scratch = &scratch;
+    pool pl;
+    memset(&pl, 0, sizeof pl);
+    pl.nthreads = 1;
+    pl.arg = s;
+
+    /* phase A over the slab and the block rows on either side (for the halo) */
+    for (int bi = row_lo - 1; bi <= row_hi; ++bi) {
+        int ri = (bi % nb + nb) % nb;
+        for (int bj = 0; bj < nb; ++bj) task_primitive(&pl, 0, ri * nb + bj);
+    }
+    int rc = 0;
+    for (int b = row_lo * nb; b < row_hi * nb && !rc; ++b) {
+        if (s->perr[b]) {
+            oracle_error* e = &a.err;
+            memset(e, 0, sizeof *e);
+            e->code = s->perr[b];
+            e->block_i = b / nb;
+            e->block_j = b % nb;
+            e->zone_i = s->pzone[b] / bs;
+            e->zone_j = s->pzone[b] % bs;
+            e->value = s->pbad[b];
+            e->x = s->xc[e->block_i * bs + e->zone_i];
+            e->y = s->xc[e->block_j * bs + e->zone_j];
+            e->time = time;
+            e->binary[0] = s->o.p1.x;
+            e->binary[1] = s->o.p1.y;
+            e->binary[2] = s->o.p2.x;
+            e->binary[3] = s->o.p2.y;
+            rc = e->code;
+        }
+    }
+    if (!rc) {
+        for (int b = row_lo * nb; b < row_hi * nb; ++b) task_fluxes(&pl, 0, b);
+        for (int b = row_lo * nb; b < row_hi * nb; ++b) task_update(&pl, 0, b);
+        if (base_cons) {
+            double w1 = -bf + 1.0;
+            size_t z0 = (size_t)row_lo * nb * n * nf, z1 = (size_t)row_hi * nb * n * nf;
+            for (size_t k = z0; k < z1; ++k) cons_out[k] = cons_out[k] * w1 + base_cons[k] * bf;
+            if (led_out && led_base) {
+                size_t l0 = (size_t)row_lo * nb * NITEMS * nf, l1 = (size_t)row_hi * nb * NITEMS * nf;
+                for (size_t k = l0; k < l1; ++k) led_out[k] = led_out[k] * w1 + led_base[k] * bf;
+            }
+        }
+    } else if (err) {
+        *err = a.err;
+    }
+    free(scratch);
     free(s->xc); free(s->xv); free(s->prim); free(s->perr); free(s->pbad); free(s->pzone); free(s->unbound);
     free(s->fxs); free(s->fys);
     return rc;

@@ -114,6 +114,19 @@ int oracle_advance(const oracle_config* cfg, double* cons, double* ledger,
 
 double oracle_max_signal_speed(const oracle_config* cfg, const double* cons);
 
+/* The maximum signal speed over block rows [row_lo, row_hi). */
+double oracle_max_signal_speed_rows(const oracle_config* cfg, const double* cons, int32_t row_lo,
+                                    int32_t row_hi);
+
+/* One RK stage of the blocks in block rows [row_lo, row_hi) of whole-mesh
+ * arrays (a row slab of a split mesh): reads the slab and its 2-zone halo
+ * rows of cons_in; base_cons (or NULL) with weight bf gives the RK average. */
+int oracle_stage_rows(const oracle_config* cfg, const double* cons_in, double* cons_out,
+                      const double* base_cons, double bf, const double* background,
+                      const double* led_in, double* led_out, const double* led_base,
+                      double time, double dt, int32_t row_lo, int32_t row_hi,
+                      oracle_error* err);
+
 int oracle_initial_state(const oracle_config* cfg, const oracle_disk_model* m,
                          double* cons);
 
