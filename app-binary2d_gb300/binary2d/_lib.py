@@ -97,6 +97,11 @@ _SIGNATURES = [
     ("b2d_stage_noalloc", c_int32, [ctypes.POINTER(B2DConfig), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                     ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, c_double,
                                     c_double, c_double, ctypes.c_void_p, ctypes.POINTER(B2DError), ctypes.c_void_p]),
+    ("b2d_set_slab", c_int32, [ctypes.c_void_p, c_int32, c_int32, c_int32]),
+    ("b2d_slab_begin", c_int32, [ctypes.c_void_p, c_int32, c_dp]),
+    ("b2d_slab_stage", c_int32, [ctypes.c_void_p]),
+    ("b2d_slab_end", c_int32, [ctypes.c_void_p, c_dp, ctypes.POINTER(B2DError)]),
+    ("b2d_slab_rows", c_int32, [ctypes.c_void_p, c_int32, c_int32, c_int32, c_dp, c_int32]),
     ("b2d_autotune", c_int32, [ctypes.c_void_p, c_int32, c_int32, ctypes.POINTER(c_int32), ctypes.POINTER(c_int32), c_dp]),
 ]
 

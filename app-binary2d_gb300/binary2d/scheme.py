@@ -236,6 +236,42 @@ class Runtime:
         _check(st)
         return dts
 
+    # -- row slabs (one run split across contexts) ------------------------------
+    def set_slab(self, run: int, block_row_lo: int, block_row_hi: int):
+        """Make block rows [lo, hi) of `run` this context's slab ((0, 0): the
+        whole run); FP64 precision only."""
+        _check(self.lib.b2d_set_slab(self.ctx, run, int(block_row_lo), int(block_row_hi)))
+
+    def slab_begin(self, fold: int, amax):
+        """Start an advance whose dt comes from amax (one global maximum signal
+        speed per run, the max over all slabs)."""
+        a = np.ascontiguousarray(np.atleast_1d(np.asarray(amax, dtype=np.float64)))
+        _check(self.lib.b2d_slab_begin(self.ctx, int(fold), _dp(a)))
+
+    def slab_stage(self):
+        _check(self.lib.b2d_slab_stage(self.ctx))
+
+    def slab_end(self) -> np.ndarray:
+        dts = np.zeros(len(self.runs), dtype=np.float64)
+        err = B2DError()
+        st = self.lib.b2d_slab_end(self.ctx, _dp(dts), ctypes.byref(err))
+        if st in (1, 2, 3):
+            raise HydroError(err)
+        _check(st)
+        return dts
+
+    def slab_rows(self, run: int, row0: int, nrows: int) -> np.ndarray:
+        """Zone rows [row0, row0 + nrows) (periodic) of the next stage's input:
+        [nf, nrows, N] FP64."""
+        N = self.runs[run].mesh.zones_per_side()
+        out = np.empty((self.nf, nrows, N), dtype=np.float64)
+        _check(self.lib.b2d_slab_rows(self.ctx, run, int(row0), int(nrows), _dp(out), 0))
+        return out
+
+    def put_slab_rows(self, run: int, row0: int, rows: np.ndarray):
+        r = np.ascontiguousarray(rows, dtype=np.float64)
+        _check(self.lib.b2d_slab_rows(self.ctx, run, int(row0), r.shape[1], _dp(r), 1))
+
     # -- tuning / introspection ----------------------------------------------
     def set_tile(self, w: int = 0, h: int = 0):
         _check(self.lib.b2d_set_tile(self.ctx, w, h))

@@ -141,8 +141,11 @@ __global__ void max_speed_kernel(const RunDev* runs, int run, int slot)
 {
     const RunDev& rd = runs[run];
     const size_t nn = (size_t)rd.N * rd.N;
+    // a row slab's zones only (its block rows are contiguous in the planes)
+    const size_t z0 = rd.slab_hi > 0 ? (size_t)rd.slab_lo * rd.bs * rd.N : 0;
+    const size_t z1 = rd.slab_hi > 0 ? (size_t)rd.slab_hi * rd.bs * rd.N : nn;
     R a = R(0);
-    for (size_t z = blockIdx.x * (size_t)blockDim.x + threadIdx.x; z < nn; z += (size_t)gridDim.x * blockDim.x) {
+    for (size_t z = z0 + blockIdx.x * (size_t)blockDim.x + threadIdx.x; z < z1; z += (size_t)gridDim.x * blockDim.x) {
         R u[NF];
         for (int f = 0; f < NF; ++f) {
             if (STORE == 0) u[f] = (R)((const double*)rd.slot[slot])[f * nn + z];
@@ -279,6 +282,9 @@ struct b2d_ctx {
     int nruns = 0, nf = 3, precision = 0, hydro = 0, rk = 2;
     int tw = 64, th = 64;
     int strip_rows = 0;   // > 0: the paired FP32 kernel covers column strips in row chunks of at most this many rows
+    // a slab advance in progress (b2d_slab_begin .. b2d_slab_end)
+    std::vector<StagePlan> slab_plan;
+    int slab_fold = 0, slab_start = -1, slab_final = -1, slab_next = -1;
     int cur = 0;
     std::vector<RunHost> runs;
     std::vector<RunDev> rdev_h;
@@ -485,7 +491,7 @@ static b2d_status sync_rundev(b2d_ctx* ctx)
     for (int i = 0; i < ctx->nruns; ++i) {
         RunHost& r = ctx->runs[i];
         RunDev& d = ctx->rdev_h[i];
-        d.tiles_i = row_chunks(ctx, r);
+        d.tiles_i = d.slab_hi > 0 ? (d.slab_hi - d.slab_lo) * (r.bs / ctx->th) : row_chunks(ctx, r);
         d.tiles_j = r.N / ctx->tw;
         d.ntiles = d.tiles_i * d.tiles_j;
         d.tile_base = base;
@@ -962,6 +968,7 @@ __global__ void elements_de_kernel(const RunDev* runs, int nstages, unsigned lon
     const int id = blockIdx.x * blockDim.x + threadIdx.x;   // block * 4 + item
     if (s >= nstages || id >= rd.nblocks * 4 || !rd.stage_ds || !rd.stage_de) return;
     const int block = id >> 2, item = id & 3;
+    if (rd.slab_hi > 0 && (block / rd.nb < rd.slab_lo || block / rd.nb >= rd.slab_hi)) return;   // another slab's
     const int nf = rd.p.hydro == B2D_EULER ? 4 : 3;
     const double* ds = rd.stage_ds + ((size_t)s * rd.nblocks + block) * NITEMS * nf + item * nf;
     const double* orbit = rd.orbit + 10 * s;
@@ -985,6 +992,7 @@ __global__ void elements_sum_kernel(const RunDev* runs, int fold, int rk, int st
     const int id = blockIdx.x * blockDim.x + threadIdx.x;   // block * 28 + item * 4 + component
     if (id >= rd.nblocks * NITEMS * 4 || !rd.stage_de || !rd.elements[start]) return;
     const int block = id / (NITEMS * 4), k = id % (NITEMS * 4), item = k / 4;
+    if (rd.slab_hi > 0 && (block / rd.nb < rd.slab_lo || block / rd.nb >= rd.slab_hi)) return;
     double e[NSLOTS];
     e[start] = rd.elements[start][id];
     int s = 0;
@@ -1197,6 +1205,19 @@ static b2d_status launch_tracers(b2d_ctx* ctx, const StagePlan& sp, bool count)
     return B2D_OK;
 }
 
+// The two per-advance orbital-element kernels (after the stage kernels).
+static b2d_status launch_elements(b2d_ctx* ctx, int fold, int start, int nstages, bool count)
+{
+    const dim3 dg((unsigned)((max_blocks(ctx) * 4 + 127) / 128), (unsigned)nstages, (unsigned)ctx->nruns);
+    elements_de_kernel<<<dg, 128, 0, ctx->stream>>>(ctx->rdev, nstages, ctx->d_err_key);
+    CUDA_TRY(cudaGetLastError());
+    const dim3 sg((unsigned)((max_blocks(ctx) * NITEMS * 4 + 127) / 128), (unsigned)ctx->nruns);
+    elements_sum_kernel<<<sg, 128, 0, ctx->stream>>>(ctx->rdev, fold, ctx->rk, start);
+    CUDA_TRY(cudaGetLastError());
+    if (count) ctx->launches += 2;
+    return B2D_OK;
+}
+
 static b2d_status enqueue_advance(b2d_ctx* ctx, int fold, int start, int* final_slot, bool count)
 {
     std::vector<StagePlan> plan = plan_advance(ctx->rk, fold, start, final_slot);
@@ -1221,15 +1242,7 @@ static b2d_status enqueue_advance(b2d_ctx* ctx, int fold, int start, int* final_
         st = launch_tracers(ctx, plan[s], count);
         if (st != B2D_OK) return st;
     }
-    const int nstages = (int)plan.size();
-    const dim3 dg((unsigned)((max_blocks(ctx) * 4 + 127) / 128), (unsigned)nstages, (unsigned)ctx->nruns);
-    elements_de_kernel<<<dg, 128, 0, ctx->stream>>>(ctx->rdev, nstages, ctx->d_err_key);
-    CUDA_TRY(cudaGetLastError());
-    const dim3 sg((unsigned)((max_blocks(ctx) * NITEMS * 4 + 127) / 128), (unsigned)ctx->nruns);
-    elements_sum_kernel<<<sg, 128, 0, ctx->stream>>>(ctx->rdev, fold, ctx->rk, start);
-    CUDA_TRY(cudaGetLastError());
-    if (count) ctx->launches += 2;
-    return B2D_OK;
+    return launch_elements(ctx, fold, start, (int)plan.size(), count);
 }
 
 extern "C" b2d_status b2d_set_tracers(b2d_ctx* ctx, int32_t run, int64_t n, const double* xy)
@@ -1686,6 +1699,110 @@ extern "C" b2d_status b2d_autotune(b2d_ctx* ctx, int32_t fold, int32_t reps, int
     if (tile_w) *tile_w = best_w;
     if (tile_h) *tile_h = best_h;
     if (ms_per_stage) *ms_per_stage = best;
+    return B2D_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Row slabs: one run split across contexts (one per GPU or process), each of
+// which advances the blocks of its own block rows.  No counterpart in the
+// reference, which advances every block of a run in one process; its block
+// dataflow joins each block with its 3x3 neighbours and extends a 2-zone
+// halo (src/scheme.rs:119-133, periodic neighbours src/mesh.rs:101-110), so a
+// slab needs the 2 zone rows on either side of it from the neighbouring slabs
+// before every stage, the global maximum signal speed for dt once per
+// advance, and its blocks' ledgers summed with the others' by the caller.
+
+extern "C" b2d_status b2d_set_slab(b2d_ctx* ctx, int32_t run, int32_t block_row_lo, int32_t block_row_hi)
+{
+    if (!ctx || run < 0 || run >= ctx->nruns) return fail(B2D_ERR_INVALID, "bad arguments");
+    RunDev& d = ctx->rdev_h[run];
+    const bool whole = block_row_lo == 0 && block_row_hi == 0;
+    if (!whole && (block_row_lo < 0 || block_row_hi > d.nb || block_row_lo >= block_row_hi))
+        return fail(B2D_ERR_INVALID, "slab rows must satisfy 0 <= lo < hi <= num_blocks");
+    if (!whole && ctx->precision != B2D_PREC_FP64)
+        return fail(B2D_ERR_UNSUPPORTED, "row slabs run on the FP64 kernel (block-aligned tiles) only");
+    CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    d.slab_lo = whole ? 0 : block_row_lo;
+    d.slab_hi = whole ? 0 : block_row_hi;
+    b2d_status st = sync_rundev(ctx);
+    if (st != B2D_OK) return st;
+    // the stored maximum signal speed becomes the slab's
+    st = launch_max_speed(ctx, run, ctx->cur);
+    if (st != B2D_OK) return st;
+    CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return B2D_OK;
+}
+
+extern "C" b2d_status b2d_slab_begin(b2d_ctx* ctx, int32_t fold, const double* amax)
+{
+    if (!ctx || fold < 1 || !amax) return fail(B2D_ERR_INVALID, "bad arguments");
+    if (ctx->slab_next >= 0) return fail(B2D_ERR_INVALID, "a slab advance is already in progress");
+    if (fold * ctx->rk > 1023) return fail(B2D_ERR_INVALID, "fold x rk_order must be at most 1023");
+    b2d_status st = ensure_stage_capacity(ctx, fold);
+    if (st != B2D_OK) return st;
+    // dt comes from the maximum signal speed over every slab of each run
+    std::vector<unsigned long long> bits(ctx->nruns);
+    memcpy(bits.data(), amax, sizeof(double) * ctx->nruns);
+    CUDA_TRY(cudaMemcpyAsync(ctx->d_amax, bits.data(), sizeof(unsigned long long) * ctx->nruns, cudaMemcpyHostToDevice,
+                             ctx->stream));
+    const int start = ctx->cur;
+    ctx->slab_plan = plan_advance(ctx->rk, fold, start, &ctx->slab_final);
+    ctx->slab_fold = fold;
+    ctx->slab_start = start;
+    ctx->slab_next = 0;
+    ctx->window.emplace_back(start, ctx->slab_plan);
+    prologue_kernel<<<ctx->nruns, 32, 0, ctx->stream>>>(ctx->rdev, fold, ctx->rk, start, ctx->slab_final, ctx->d_err_key,
+                                                         ctx->d_adv_count);
+    CUDA_TRY(cudaGetLastError());
+    ctx->launches++;
+    CUDA_TRY(cudaStreamSynchronize(ctx->stream));   // bits is host memory of this call
+    return B2D_OK;
+}
+
+extern "C" b2d_status b2d_slab_stage(b2d_ctx* ctx)
+{
+    if (!ctx || ctx->slab_next < 0 || ctx->slab_next >= (int)ctx->slab_plan.size())
+        return fail(B2D_ERR_INVALID, "no slab stage left to run");
+    const int s = ctx->slab_next;
+    b2d_status st = launch_stage(ctx, ctx->slab_plan[s], s, s + 1 == (int)ctx->slab_plan.size());
+    if (st != B2D_OK) return st;
+    ctx->launches++;
+    st = launch_tracers(ctx, ctx->slab_plan[s], true);
+    if (st != B2D_OK) return st;
+    ctx->slab_next++;
+    return B2D_OK;
+}
+
+extern "C" b2d_status b2d_slab_end(b2d_ctx* ctx, double* dt_out, b2d_error* err_out)
+{
+    if (!ctx || ctx->slab_next != (int)ctx->slab_plan.size() || ctx->slab_plan.empty())
+        return fail(B2D_ERR_INVALID, "the slab advance has stages left to run");
+    b2d_status st = launch_elements(ctx, ctx->slab_fold, ctx->slab_start, (int)ctx->slab_plan.size(), true);
+    ctx->slab_next = -1;
+    if (st != B2D_OK) return st;
+    return finish_advance(ctx, ctx->slab_final, dt_out, err_out);
+}
+
+extern "C" b2d_status b2d_slab_rows(b2d_ctx* ctx, int32_t run, int32_t row0, int32_t nrows, double* rows, int32_t put)
+{
+    if (!ctx || run < 0 || run >= ctx->nruns || !rows || nrows < 1) return fail(B2D_ERR_INVALID, "bad arguments");
+    if (ctx->precision != B2D_PREC_FP64) return fail(B2D_ERR_UNSUPPORTED, "row exchange of the FP64 state only");
+    RunHost& r = ctx->runs[run];
+    if (nrows > r.N) return fail(B2D_ERR_INVALID, "more rows than the mesh has");
+    // the next stage's input slot, or the current state between advances
+    const int slot = ctx->slab_next >= 0 && ctx->slab_next < (int)ctx->slab_plan.size()
+                         ? ctx->slab_plan[ctx->slab_next].in : ctx->cur;
+    const size_t nn = (size_t)r.N * r.N;
+    double* planes = (double*)r.slot[slot];
+    for (int f = 0; f < ctx->nf; ++f)
+        for (int k = 0; k < nrows; ++k) {
+            const int gi = ((row0 + k) % r.N + r.N) % r.N;
+            double* dev = planes + f * nn + (size_t)gi * r.N;
+            double* host = rows + ((size_t)f * nrows + k) * r.N;
+            if (put) CUDA_TRY(cudaMemcpyAsync(dev, host, sizeof(double) * r.N, cudaMemcpyHostToDevice, ctx->stream));
+            else CUDA_TRY(cudaMemcpyAsync(host, dev, sizeof(double) * r.N, cudaMemcpyDeviceToHost, ctx->stream));
+        }
+    CUDA_TRY(cudaStreamSynchronize(ctx->stream));
     return B2D_OK;
 }
 

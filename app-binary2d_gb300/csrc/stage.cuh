@@ -172,7 +172,8 @@ __global__ void __launch_bounds__(256) stage_kernel(StageArgs a)
     const int N = rd.N, bs = rd.bs;
     const size_t nn = (size_t)N * N;
     const int lt = g - rd.tile_base;
-    const int tj = lt % rd.tiles_j, ti = lt / rd.tiles_j;
+    const int tj = lt % rd.tiles_j;
+    const int ti = lt / rd.tiles_j + (rd.slab_hi > 0 ? rd.slab_lo * (bs / TH) : 0);   // tile rows of the slab
     const int i0 = ti * TH, j0 = tj * TW;
     const int bi = i0 / bs, bj = j0 / bs, li0 = i0 % bs, lj0 = j0 % bs;
     const int block = bi * rd.nb + bj;

@@ -433,18 +433,28 @@ def ours(args):
     rt.transfers_wait(0)
     rt.synchronize()
     barrier()
+    # three trials of the timed loop; the reported figure is the median trial.
+    # The host link of these GPUs is shared with other tenants of the machine:
+    # a trial's copies can run at a fraction of the link rate while the
+    # advance on the device does not change, so one trial alone may be an
+    # outlier (every trial is listed in the JSON line)
     e2e_steps = max(4, args.steps // 2)
-    t0 = time.perf_counter()
-    for k in range(e2e_steps):
-        e2e_step(k)
-    rt.transfers_wait(0)
-    rt.synchronize()
-    el = time.perf_counter() - t0
-    if dist:
-        t = torch.tensor([el], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        el = float(t.item())
-    e2e_value = zones * FOLD * e2e_steps / el * ws
+    trials = []
+    for _ in range(3):
+        barrier()
+        t0 = time.perf_counter()
+        for k in range(e2e_steps):
+            e2e_step(k)
+        rt.transfers_wait(0)
+        rt.synchronize()
+        el = time.perf_counter() - t0
+        if dist:
+            t = torch.tensor([el], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            el = float(t.item())
+        trials.append(zones * FOLD * e2e_steps / el * ws)
+    e2e_value = statistics.median(trials)
+    copy_gbs_after = link_bandwidth(torch, host_in[0], host_out[0])
     rt.close()
     for a in host_in + host_out:
         b2.unpin(a)
@@ -503,7 +513,8 @@ def ours(args):
             "accuracy": accuracy,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(cons.nbytes),
-                    "d2h_bytes_per_step": int(cons.nbytes), "link_gbs": copy_gbs},
+                    "d2h_bytes_per_step": int(cons.nbytes), "trials": trials, "steps_per_trial": e2e_steps,
+                    "statistic": "median of the trials", "link_gbs": copy_gbs, "link_gbs_after": copy_gbs_after},
             "gpu_launches": int(launches),
             "clocks": clk.summary(),
         }

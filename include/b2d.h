@@ -345,6 +345,48 @@ b2d_status b2d_unpin_host(void* ptr);
 b2d_status b2d_set_device(int32_t device);
 
 /* ------------------------------------------------------------------------ */
+/* Row slabs: one run split across contexts (one per GPU or process), each
+ * advancing the blocks of its own block rows.  No counterpart in the
+ * reference, which advances every block of a run in one process; its block
+ * dataflow joins each block with its 3x3 neighbours and extends a 2-zone
+ * halo (src/scheme.rs:119-133; periodic neighbours, src/mesh.rs:101-110), so
+ * an advance of a split run is, per context:
+ *   1. b2d_max_signal_speed of each context's slab, reduced with max over
+ *      the contexts (State::max_signal_speed, src/state.rs:121-133);
+ *   2. b2d_slab_begin(fold, global maxima): dt and the stage times;
+ *   3. per stage: exchange halo rows — b2d_slab_rows(get) of the slab's first
+ *      and last two zone rows, b2d_slab_rows(put) of the neighbours' into the
+ *      two rows above and below the slab (periodically) — then b2d_slab_stage;
+ *   4. b2d_slab_end: the orbital-element ledger of the slab's blocks, dt and
+ *      errors as b2d_advance reports them.
+ * The per-block ledgers of the slab's blocks are this context's; a caller
+ * sums them with the other slabs' (each block has one owner).  The results
+ * equal an unsplit run's bit for bit.  FP64 precision only (block-aligned
+ * tiles of the FP64 kernel). */
+
+/* Make block rows [block_row_lo, block_row_hi) of `run` this context's slab
+ * ((0, 0): the whole run again).  The stage kernel then covers only the
+ * slab's tiles, b2d_max_signal_speed the slab's zones (recomputed here), and
+ * the orbital-element ledger the slab's blocks. */
+b2d_status b2d_set_slab(b2d_ctx* ctx, int32_t run, int32_t block_row_lo, int32_t block_row_hi);
+
+/* Start an advance of `fold` RK steps whose dt comes from amax[run], the
+ * maximum signal speed of each run over all of its slabs. */
+b2d_status b2d_slab_begin(b2d_ctx* ctx, int32_t fold, const double* amax);
+
+/* Run the next RK stage of the advance begun by b2d_slab_begin. */
+b2d_status b2d_slab_stage(b2d_ctx* ctx);
+
+/* Finish the advance after its last stage (as b2d_advance returns: dt of
+ * each run, hydro errors with the state kept as it was before the advance). */
+b2d_status b2d_slab_end(b2d_ctx* ctx, double* dt_out, b2d_error* err_out);
+
+/* Copy zone rows [row0, row0 + nrows) (periodic) of the next stage's input
+ * (between advances: of the current state) to (put = 0) or from (put = 1)
+ * `rows`, laid out [nf][nrows][N] in FP64. */
+b2d_status b2d_slab_rows(b2d_ctx* ctx, int32_t run, int32_t row0, int32_t nrows, double* rows, int32_t put);
+
+/* ------------------------------------------------------------------------ */
 /* One RK stage that allocates nothing.  No counterpart in the reference: it
  * serves callers that cannot call cudaMalloc — a host code that owns a fixed
  * device memory pool and forbids allocation by libraries, or an
