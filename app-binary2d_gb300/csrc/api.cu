@@ -498,7 +498,9 @@ static b2d_status sync_rundev(b2d_ctx* ctx)
         // partial slots of the block with the most chunk pieces (every block:
         // bs / th for block-aligned tiles)
         int most = 0;
-        for (int b = 0; b < r.nb; ++b) most = std::max(most, chunks_in_block_row(b, r.bs, r.N, d.tiles_i));
+        if (d.slab_hi > 0) most = r.bs / ctx->th;   // a slab's tiles are block-aligned
+        else
+            for (int b = 0; b < r.nb; ++b) most = std::max(most, chunks_in_block_row(b, r.bs, r.N, d.tiles_i));
         d.tiles_per_block = most * std::max(r.bs / ctx->tw, 1);
         base += d.ntiles;
         CUDA_TRY(cudaFree(r.partial));

@@ -10,6 +10,7 @@ Two steps, because the oracle's orbit costs up to 8e10 zone-updates:
     (--workload euler --side 512 --fold 1 for the Euler disk, whose dt falls by
     3.6x in its first steps: one dt for ten of them breaks the CFL condition)
     python tests/orbit_accuracy.py compare --workload disk_8192 --steps 1000 [--json OUT]
+    python tests/orbit_accuracy.py orbit --workload euler --side 4096 [--json OUT]
 
 The first runs the oracle for one orbit (fold 10 advances until t >= 2π) and
 caches Σ at the end and the time series of the domain totals of the
@@ -40,7 +41,9 @@ ITEMS = ("sink1", "sink2", "grav1", "grav2", "buffer", "cooling", "fake_mass")
 def _case(side, workload="disk"):
     import binary2d as b2
     if workload == "euler":
-        mesh, hydro, physics, model = b2.presets.euler_beta_disk(side // 64, 64)
+        # the workload's 128^2 blocks at full size (32 x 32 at 4096^2), 64^2 blocks at the oracle's sizes
+        nb, bs = (side // 128, 128) if side >= 1024 else (side // 64, 64)
+        mesh, hydro, physics, model = b2.presets.euler_beta_disk(nb, bs)
     elif workload == "disk_8192":
         mesh, hydro, physics, model = b2.presets.disk_8192()[:4]
     elif side == 2048:
@@ -154,6 +157,39 @@ def run_compare(args):
     print(json.dumps(out))
 
 
+def run_orbit(args):
+    """One orbit of the FP32 path alone on the full-size workload (the Euler
+    beta-cooling disk at 4096^2: the oracle cannot follow it), with the run's
+    end state: time reached, hydro status, finiteness, accreted mass."""
+    import binary2d as b2
+    mesh, hydro, physics, cons = _case(args.side, args.workload)
+    t0 = time.time()
+    status = "ok"
+    with b2.Runtime([b2.Run(mesh, hydro, physics)], precision=args.precision) as rt:
+        tile = rt.autotune()
+        rows = rt.strip_rows()
+        rt.upload(0, cons)
+        n = 0
+        try:
+            while rt.time(0)[0] < args.orbits * 2 * np.pi:
+                rt.advance(args.fold)
+                n += 1
+        except b2.HydroError as e:
+            status = "%s at t=%.5f, block %s" % (e.kind, e.time, e.block)
+        t, it = rt.time(0)
+        s = rt.download(0)[0]
+        led = rt.ledger(0)
+    out = {"workload": "%s %d^2" % (args.workload, args.side), "precision": args.precision, "fold": args.fold,
+           "cfl": physics.cfl, "advances": n, "steps": it, "t_end": t, "orbits": t / (2 * np.pi), "status": status,
+           "seconds": time.time() - t0, "tile": [tile[0], tile[1]], "strip_rows": rows,
+           "state_finite": bool(np.isfinite(s).all()), "sigma_min": float(s[..., 0].min()),
+           "sigma_max": float(s[..., 0].max()), "accreted_mass": float(-led[:, :, 0:2, 0].sum())}
+    if args.json:
+        with open(args.json, "w") as f:
+            json.dump(out, f, indent=1)
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     sub = ap.add_subparsers(dest="cmd", required=True)
@@ -171,8 +207,15 @@ def main():
     c.add_argument("--workload", default="disk_8192", choices=["disk_8192"])
     c.add_argument("--steps", type=int, default=1000)
     c.add_argument("--json", default="")
+    r = sub.add_parser("orbit")
+    r.add_argument("--workload", default="euler", choices=["euler", "disk"])
+    r.add_argument("--side", type=int, default=4096)
+    r.add_argument("--orbits", type=float, default=1.0)
+    r.add_argument("--fold", type=int, default=FOLD)
+    r.add_argument("--precision", default="fp32_comp", choices=["fp64", "fp32_state64", "fp32_comp"])
+    r.add_argument("--json", default="")
     args = ap.parse_args()
-    {"oracle": run_oracle, "gpu": run_gpu, "compare": run_compare}[args.cmd](args)
+    {"oracle": run_oracle, "gpu": run_gpu, "compare": run_compare, "orbit": run_orbit}[args.cmd](args)
 
 
 if __name__ == "__main__":
