@@ -161,8 +161,23 @@ def run_orbit(args):
     """One orbit of the FP32 path alone on the full-size workload (the Euler
     beta-cooling disk at 4096^2: the oracle cannot follow it), with the run's
     end state: time reached, hydro status, finiteness, accreted mass."""
+    import dataclasses
     import binary2d as b2
     mesh, hydro, physics, cons = _case(args.side, args.workload)
+    # open parameters changed from the preset: --physics key=value, --model key=value
+    def parse(items):
+        out = {}
+        for kv in items:
+            k, v = kv.split("=", 1)
+            out[k] = None if v == "none" else float(v)
+        return out
+    if args.physics or args.model:
+        nb, bs = (args.side // 128, 128) if args.side >= 1024 else (args.side // 64, 64)
+        mesh, hydro, physics, model = b2.presets.euler_beta_disk(nb, bs) if args.workload == "euler" else \
+            b2.presets.iso_disk(nb, bs, seed=1)
+        physics = dataclasses.replace(physics, **parse(args.physics))
+        model = dataclasses.replace(model, **parse(args.model))
+        cons = b2.initial_state(mesh, hydro, physics, model)
     t0 = time.time()
     status = "ok"
     with b2.Runtime([b2.Run(mesh, hydro, physics)], precision=args.precision) as rt:
@@ -179,7 +194,8 @@ def run_orbit(args):
         t, it = rt.time(0)
         s = rt.download(0)[0]
         led = rt.ledger(0)
-    out = {"workload": "%s %d^2" % (args.workload, args.side), "precision": args.precision, "fold": args.fold,
+    out = {"workload": "%s %d^2" % (args.workload, args.side), "changed": {"physics": args.physics, "model": args.model},
+           "precision": args.precision, "fold": args.fold,
            "cfl": physics.cfl, "advances": n, "steps": it, "t_end": t, "orbits": t / (2 * np.pi), "status": status,
            "seconds": time.time() - t0, "tile": [tile[0], tile[1]], "strip_rows": rows,
            "state_finite": bool(np.isfinite(s).all()), "sigma_min": float(s[..., 0].min()),
@@ -213,6 +229,8 @@ def main():
     r.add_argument("--orbits", type=float, default=1.0)
     r.add_argument("--fold", type=int, default=FOLD)
     r.add_argument("--precision", default="fp32_comp", choices=["fp64", "fp32_state64", "fp32_comp"])
+    r.add_argument("--physics", nargs="*", default=[], help="Physics fields to change, key=value")
+    r.add_argument("--model", nargs="*", default=[], help="DiskModel fields to change, key=value")
     r.add_argument("--json", default="")
     args = ap.parse_args()
     {"oracle": run_oracle, "gpu": run_gpu, "compare": run_compare, "orbit": run_orbit}[args.cmd](args)
