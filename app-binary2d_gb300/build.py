@@ -6,6 +6,7 @@ into app-binary2d_gb300/_build/libb2d.so.  Flags per unit:
   kernels_f64.cu   --fmad=false   FP64 parity kernels: every operation rounds as written
   api.cu           --fmad=false   Kepler solve and time bookkeeping in exact FP64
   kernels_f32.cu   fast FP32      -ftz, approximate division and square root
+  kernels_f32e.cu  fast FP32      the paired Euler kernel, same flags
   host_ic.cpp      g++ -ffp-contract=off   geometry and initial states
 """
 import concurrent.futures as cf
@@ -31,6 +32,7 @@ UNITS = {
     "kernels_f64.cu": ["--fmad=false"],
     "api.cu": ["--fmad=false"],
     "kernels_f32.cu": ["-ftz=true", "-prec-div=false", "-prec-sqrt=false", "--fmad=true"],
+    "kernels_f32e.cu": ["-ftz=true", "-prec-div=false", "-prec-sqrt=false", "--fmad=true"],
 }
 HOST_UNITS = {"host_ic.cpp": ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-pthread"]}
 

@@ -418,9 +418,9 @@ static int default_tile_w(int bs)
 
 static bool tile_ok(const b2d_ctx* ctx, int tw, int th)
 {
-    // the paired FP32 kernel's 128-, 256- and 512-column tiles may also span
+    // the paired FP32 kernels' 128-, 256- and 512-column tiles may also span
     // whole blocks side by side (blocks of 64 columns or more)
-    const bool span = ctx->precision == B2D_PREC_FP32_COMP && ctx->nf == 3 && (tw == 128 || tw == 256 || tw == 512);
+    const bool span = ctx->precision == B2D_PREC_FP32_COMP && (tw == 128 || tw == 256 || tw == 512);
     if (tw < 1 || th < 1 || tw > (span ? 512 : 256)) return false;
     for (const RunHost& r : ctx->runs) {
         if (r.bs % th) return false;
@@ -464,13 +464,13 @@ static void free_ctx(b2d_ctx* ctx)
 
 // Rebuild the tile bookkeeping for the current tile shape and push the run
 // descriptors to the device.
-// The stage kernel the context launches takes row chunks: the paired-column
+// The stage kernel the context launches takes row chunks: a paired-column
 // kernel or the TMA-staged one (launch_stage_f32 makes the same choice), not
 // the FP64 or the generic kernel.
 static bool chunk_kernel(const b2d_ctx* ctx)
 {
     if (ctx->precision == B2D_PREC_FP64) return false;
-    if (ctx->precision == B2D_PREC_FP32_COMP && ctx->nf == 3 &&
+    if (ctx->precision == B2D_PREC_FP32_COMP &&
         (ctx->tw == 64 || ctx->tw == 128 || ctx->tw == 256 || ctx->tw == 512))
         return true;
     return ctx->tw % 32 == 0 && ctx->tw <= 128;
@@ -1642,7 +1642,7 @@ extern "C" b2d_status b2d_autotune(b2d_ctx* ctx, int32_t fold, int32_t reps, int
     b2d_status st = ensure_stage_capacity(ctx, fold);
     if (st != B2D_OK) return st;
     CUDA_TRY(cudaStreamSynchronize(ctx->stream));
-    const int max_w = ctx->precision == B2D_PREC_FP64 || (ctx->precision == B2D_PREC_FP32_COMP && ctx->nf == 3) ? 256 : 128;
+    const int max_w = ctx->precision == B2D_PREC_FP64 || ctx->precision == B2D_PREC_FP32_COMP ? 256 : 128;
     int best_w = ctx->tw, best_h = ctx->th, best_rows = 0;
     double best = 1e300;
     ctx->strip_rows = 0;

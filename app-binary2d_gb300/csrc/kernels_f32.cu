@@ -1,6 +1,7 @@
 // kernels_f32.cu — FP32-stencil stage kernels over FP64 state (store 0) or
-// compensated FP32 state (store 1).  Isothermal compensated tiles 64, 128,
-// 256 or 512 columns wide run the paired-column kernel of stage3.cuh; other tiles
+// compensated FP32 state (store 1).  Compensated tiles 64, 128, 256 or 512
+// columns wide run the paired-column kernels: stage3.cuh (isothermal) and
+// stage3e.cuh (Euler, kernels_f32e.cu); other tiles
 // whose width is a multiple of 32 (at most 128) run the TMA-staged kernel of
 // stage2.cuh; narrower tiles (blocks of fewer than 32 zones) run the generic
 // kernel of stage.cuh.  The first two take row chunks across block rows.
@@ -8,6 +9,11 @@
 #include "stage3.cuh"
 
 namespace b2d {
+
+// the paired Euler kernel (kernels_f32e.cu)
+bool euler_paired_width(int tw);
+int euler_paired_ctas_per_sm(int nruns, int tw);
+cudaError_t launch_euler_paired(const StageArgs& a, int grid, int tw, cudaStream_t s);
 
 template <int NF, int STORE, bool SINGLE>
 static cudaError_t launch_two_impl(const StageArgs& a, int grid, int tw, cudaStream_t s)
@@ -57,6 +63,7 @@ static int two_ctas_per_sm(int nruns, int tw)
 int stage_ctas_per_sm(int nf, int store, int nruns, int tw)
 {
     int n = 0;
+    if (nf == 4 && store == 1 && euler_paired_width(tw)) return euler_paired_ctas_per_sm(nruns, tw);
     if (nf == 3 && store == 1 && (tw == 64 || tw == 128 || tw == 256 || tw == 512)) {
         const size_t smem = s3_smem_bytes(tw);
         void (*k)(StageArgs);
@@ -77,6 +84,7 @@ int stage_ctas_per_sm(int nf, int store, int nruns, int tw)
 
 cudaError_t launch_stage_f32(int nf, int store, const StageArgs& a, int grid, int tw, size_t smem, cudaStream_t s)
 {
+    if (nf == 4 && store == 1 && euler_paired_width(tw)) return launch_euler_paired(a, grid, tw, s);
     if (nf == 3 && store == 1 && (tw == 64 || tw == 128))
         return a.nruns == 1 ? launch_three_impl<true, 128>(a, grid, tw, s)
                             : launch_three_impl<false, 128>(a, grid, tw, s);

@@ -73,7 +73,7 @@ def link_bandwidth(torch, host_src, host_dst):
 
 
 PROFILES = {("disk_2048", "fp32_comp"): "stage3_kernel_fp32comp_disk2048.md",
-            ("euler_4096", "fp32_comp"): "stage2_kernel_fp32comp_euler4096.md"}
+            ("euler_4096", "fp32_comp"): "stage3e_kernel_fp32comp_euler4096.md"}
 
 
 def ncu_profile(workload, precision, key):
