@@ -21,9 +21,10 @@
 //    cooling item carries rho de in the energy field only (see
 //    source_terms, physics.cuh); sinks per column, in warps with a zone
 //    inside a sink radius.
-//  * The ledger's group 0 (gravity, buffer, cooling: 14 live items) is
-//    summed over the warp every row into the warp's bank, as stage2.cuh
-//    does, rather than held per thread across rows.
+//  * The ledger's group 0 (gravity, buffer, cooling: 14 live items, 11 of
+//    them non-zero in FP32) is summed per thread over the tile's rows and
+//    over the warp once per ledger piece (at a crossing tile's first-piece
+//    row and after the loop).
 #pragma once
 
 #include "stage3.cuh"
@@ -54,6 +55,132 @@ __device__ __forceinline__ int euler_floors(const DevParamsF& P, float* p)
     if (P.has_pressure_floor && p[3] < P.pressure_floor) p[3] = P.pressure_floor;
     if (p[3] <= 0.0f) return 2;
     return 0;
+}
+
+// Three-input FP32 minimum and maximum (PTX min/max with three sources, sm_100+).
+__device__ __forceinline__ float min3f(float a, float b, float c)
+{
+    float d;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+__device__ __forceinline__ float max3f(float a, float b, float c)
+{
+    float d;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+
+// Generalised minmod of each lane (plm_gradient, physics.cuh) as the median of
+// min(x, y, z), max(x, y, z) and 0: the minimum when all three are positive,
+// the maximum when all are negative, else 0 — min(max(lo, 0), hi) for lo <= hi.
+__device__ __forceinline__ float2 plm_gradient2m(float2 th, float2 a, float2 b, float2 c)
+{
+    const float2 x = mul2(th, sub2(b, a));
+    const float2 y = mul2(f2(0.5f), sub2(c, a));
+    const float2 z = mul2(th, sub2(c, b));
+    return make_float2(fminf(fmaxf(min3f(x.x, y.x, z.x), 0.0f), max3f(x.x, y.x, z.x)),
+                       fminf(fmaxf(min3f(x.y, y.y, z.y), 0.0f), max3f(x.y, y.y, z.y)));
+}
+
+// e^x - 1 of two small arguments (|x| <= 0.35): the Taylor series
+// x (1 + x/2 + x^2/6 + ... + x^7/8!) in Horner form; the first omitted term,
+// x^9/9!, is below 6e-10 |x| there.
+__device__ __forceinline__ float2 expm1_small2(float2 x)
+{
+    float2 p = f2(1.0f / 40320.0f);
+    p = fma2(p, x, f2(1.0f / 5040.0f));
+    p = fma2(p, x, f2(1.0f / 720.0f));
+    p = fma2(p, x, f2(1.0f / 120.0f));
+    p = fma2(p, x, f2(1.0f / 24.0f));
+    p = fma2(p, x, f2(1.0f / 6.0f));
+    p = fma2(p, x, f2(0.5f));
+    p = fma2(p, x, f2(1.0f));
+    return mul2(p, x);
+}
+
+// Scalar FP32 pieces of the paired kernel written with explicit roundings
+// (fmaf, __fmul_rn, __fadd_rn: no contraction left to the compiler), so that
+// every instantiation of the kernel (tile widths 128, 256, 512) rounds them
+// alike and the states stay independent of the tiling.
+
+// Euler cons -> prim without floors (physics.rs:696): rho, vx, vy, p.
+__device__ __forceinline__ void euler_prim_exact(const DevParamsF& P, const float* u, float* p)
+{
+    const float ir = __fdividef(1.0f, u[0]);
+    p[0] = u[0];
+    p[1] = __fmul_rn(u[1], ir);
+    p[2] = __fmul_rn(u[2], ir);
+    const float v2 = fmaf(p[1], p[1], __fmul_rn(p[2], p[2]));
+    p[3] = __fmul_rn(fmaf(__fmul_rn(-0.5f, u[0]), v2, u[3]), P.gm1);
+}
+
+// Euler::max_signal_speed (physics.rs:679-681): max(|vx|, |vy|) + sqrt(gamma p / rho).
+__device__ __forceinline__ float euler_max_speed_exact(const DevParamsF& P, const float* u)
+{
+    float p[4];
+    euler_prim_exact(P, u, p);
+    const float cs = sqrtf(__fmul_rn(__fmul_rn(P.gamma, p[3]), __fdividef(1.0f, p[0])));
+    return __fadd_rn(fmaxf(fabsf(p[1]), fabsf(p[2])), cs);
+}
+
+// Physics::sink_kernel (physics.rs:388-397): rate (1 - r^2 / s^2)^2 inside the sink radius s.
+__device__ __forceinline__ float sink_rate_exact(const DevParamsF& P, float dx, float dy)
+{
+    const float r2 = fmaf(dx, dx, __fmul_rn(dy, dy));
+    if (r2 < P.sink_r2) {
+        const float t = fmaf(-r2, P.inv_sink_r2, 1.0f);
+        return __fmul_rn(P.sink_rate, __fmul_rn(t, t));
+    }
+    return 0.0f;
+}
+
+// The torque-free sink velocity: the gas velocity relative to the body,
+// projected on the radial direction, plus the body's velocity (physics.rs:743-756).
+__device__ __forceinline__ void torque_free_exact(const DevParamsF& P, const PointMass<float>& b, float x, float y,
+                                                  float vx, float vy, float& vxc, float& vyc)
+{
+    const float vxb = P.one_body ? 0.0f : b.vx, vyb = P.one_body ? 0.0f : b.vy;
+    const float ddx = x - b.x, ddy = y - b.y;
+    const float r = sqrtf(fmaf(ddx, ddx, __fmul_rn(ddy, ddy)));
+    const float rx = __fdividef(ddx, r), ry = __fdividef(ddy, r);
+    const float dvdotr = fmaf(vx - vxb, rx, __fmul_rn(vy - vyb, ry));
+    vxc = fmaf(dvdotr, rx, vxb);
+    vyc = fmaf(dvdotr, ry, vyb);
+}
+
+// The sink items of one Euler zone (the sink part of Euler::source_terms,
+// physics.rs:683-774): -rate u dt (impartial sinks) or -rate dt times the
+// torque-free state (rho, rho v_sink, rho e + rho v_sink^2 / 2).
+__device__ __forceinline__ void euler_sink_items(const DevParamsF& P, const Binary<float>& B, const float* u, float x,
+                                                 float y, float dt, float* s1, float* s2)
+{
+    const float sr1 = __fmul_rn(sink_rate_exact(P, x - B.p1.x, y - B.p1.y), -dt);
+    const float sr2 = __fmul_rn(sink_rate_exact(P, x - B.p2.x, y - B.p2.y), -dt);
+    if (P.sink_model == 0) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            s1[k] = __fmul_rn(u[k], sr1);
+            s2[k] = __fmul_rn(u[k], sr2);
+        }
+    } else {
+        float p[4];
+        euler_prim_exact(P, u, p);
+        const float e0 = __fmul_rn(__fdividef(p[3], p[0]), P.inv_gm1);
+        float v1x, v1y, v2x, v2y;
+        torque_free_exact(P, B.p1, x, y, p[1], p[2], v1x, v1y);
+        torque_free_exact(P, B.p2, x, y, p[1], p[2], v2x, v2y);
+        const float sd = p[0], hs = __fmul_rn(0.5f, sd);
+        const float a1[4] = {sd, __fmul_rn(sd, v1x), __fmul_rn(sd, v1y),
+                             fmaf(sd, e0, __fmul_rn(hs, fmaf(v1x, v1x, __fmul_rn(v1y, v1y))))};
+        const float a2[4] = {sd, __fmul_rn(sd, v2x), __fmul_rn(sd, v2y),
+                             fmaf(sd, e0, __fmul_rn(hs, fmaf(v2x, v2x, __fmul_rn(v2y, v2y))))};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            s1[k] = __fmul_rn(a1[k], sr1);
+            s2[k] = __fmul_rn(a2[k], sr2);
+        }
+    }
 }
 
 // 0.5 K of the alpha model at two faces (x, fy.x) and (x, fy.y)
@@ -135,7 +262,6 @@ stage3e_kernel(StageArgs a)
 {
     constexpr int NF = 4;
     constexpr int H = 4;                     // staged halo columns per side: 16 bytes of FP32
-    constexpr int NL = NITEMS * NF;
 
     const int TP = blockDim.x - 32;          // interior threads (column pairs)
     const int TW = 2 * TP;
@@ -286,6 +412,24 @@ stage3e_kernel(StageArgs a)
     for (int i = t; i < NWI * 32; i += blockDim.x) sLed[i >> 5][i & 31] = sLedA[i >> 5][i & 31] = 0.0f;
     const int slot0 = group_writer_slot<NF, 0>(lane);
     const int slot1 = group_writer_slot<NF, 1>(lane);
+    // group 0 of this pair summed over rows: grav1 (x, y, e), grav2 (x, y, e),
+    // buffer (4 fields), cooling (energy; its mass and momentum are zero)
+    float acc0[11];
+#pragma unroll
+    for (int m = 0; m < 11; ++m) acc0[m] = 0.0f;
+    // the warp's total of acc0 into a bank row, in item order, and a fresh start
+    auto flush_acc = [&](float* bank) {
+        float v[16];
+#pragma unroll
+        for (int m = 0; m < 10; ++m) v[m] = acc0[m];
+        v[10] = v[11] = v[12] = 0.0f;
+        v[13] = acc0[10];
+        v[14] = v[15] = 0.0f;
+        const float s0 = warp_sum_items<16>(v, lane);
+        if (slot0 >= 0) bank[slot0] += s0;
+#pragma unroll
+        for (int m = 0; m < 11; ++m) acc0[m] = 0.0f;
+    };
     float amax = 0.0f;
 #pragma unroll
     for (int f = 0; f < NF; ++f) { Pm1[f] = P0[f] = fxA[f] = fxB[f] = xg[f] = f2(0.0f); }
@@ -348,8 +492,8 @@ stage3e_kernel(StageArgs a)
             float2 gx[NF], gy[NF];
 #pragma unroll
             for (int f = 0; f < NF; ++f) {
-                gx[f] = plm_gradient2(thx, Pm1[f], P0[f], pn[f]);
-                gy[f] = plm_gradient2(thy, make_float2(lv[f], P0[f].x), P0[f], make_float2(P0[f].y, rv[f]));
+                gx[f] = plm_gradient2m(thx, Pm1[f], P0[f], pn[f]);
+                gy[f] = plm_gradient2m(thy, make_float2(lv[f], P0[f].x), P0[f], make_float2(P0[f].y, rv[f]));
             }
             // factored stress_field terms (physics.rs:322-340; face_flux, stage2.cuh)
             const float2 da = mul2(gx[1], f2(inv_dx)), db = mul2(gy[2], f2(inv_dx));
@@ -443,7 +587,7 @@ stage3e_kernel(StageArgs a)
                 // sources of the pair (Physics::source_terms, physics.rs:423-457;
                 // Euler::source_terms, physics.rs:683-774)
                 float2 tot[NF];
-                float v0[16];                 // ledger group 0 of the pair, in item order
+                float v0[11];                 // ledger group 0 of the pair (acc0's order)
                 bool sinks_any;
                 float led1[8];
                 {
@@ -482,7 +626,10 @@ stage3e_kernel(StageArgs a)
                         // beta-cooling: e -> e exp(-Omega dt / beta), Omega^2 = sum m / (d^2 + s^2)^(3/2)
                         const float2 om = sqrt2(fma2(f2(B.p1.m), r13, mul2(f2(B.p2.m), r23)));
                         const float2 c = mul2(om, f2(-dt * P.inv_cool_beta));
-                        dec = mul2(e0, make_float2(expm1f(c.x), expm1f(c.y)));
+                        if (__any_sync(0xffffffffu, fabsf(c.x) > 0.35f || fabsf(c.y) > 0.35f))
+                            dec = mul2(e0, make_float2(expm1f(c.x), expm1f(c.y)));
+                        else
+                            dec = mul2(e0, expm1_small2(c));
                     } else {
                         // T^4 law: e -> e (1 + 3 a e^3 dt)^(-1/3), a = coefficient / rho^n x slow start
                         float d2[2];
@@ -509,14 +656,11 @@ stage3e_kernel(StageArgs a)
                     tot[1] = add2(add2(g1x, g2x), bu[1]);
                     tot[2] = add2(add2(g1y, g2y), bu[2]);
                     tot[3] = add2(add2(add2(g1e, g2e), bu[3]), cool);
-                    // group 0 in item order: grav1 (x, y, e), grav2 (x, y, e), buffer (4), cooling (4)
                     v0[0] = g1x.x + g1x.y; v0[1] = g1y.x + g1y.y; v0[2] = g1e.x + g1e.y;
                     v0[3] = g2x.x + g2x.y; v0[4] = g2y.x + g2y.y; v0[5] = g2e.x + g2e.y;
 #pragma unroll
                     for (int f = 0; f < NF; ++f) v0[6 + f] = bu[f].x + bu[f].y;
-                    v0[10] = v0[11] = v0[12] = 0.0f;
-                    v0[13] = cool.x + cool.y;
-                    v0[14] = v0[15] = 0.0f;
+                    v0[10] = cool.x + cool.y;
 #pragma unroll
                     for (int m = 0; m < 8; ++m) led1[m] = 0.0f;
                     // sinks: only where a zone of the warp lies inside a sink radius
@@ -524,21 +668,19 @@ stage3e_kernel(StageArgs a)
                     const bool near = s1.x < P.sink_r2 || s1.y < P.sink_r2 || s2.x < P.sink_r2 || s2.y < P.sink_r2;
                     sinks_any = __any_sync(0xffffffffu, near);
                     if (sinks_any) {
-                        float it[NL];
-#pragma unroll
+#pragma unroll 1
                         for (int side = 0; side < 2; ++side) {
                             const float us[NF] = {side ? uc[0].y : uc[0].x, side ? uc[1].y : uc[1].x,
                                                   side ? uc[2].y : uc[2].x, side ? uc[3].y : uc[3].x};
-                            const float u0s[NF] = {side ? u0[0].y : u0[0].x, side ? u0[1].y : u0[1].x,
-                                                   side ? u0[2].y : u0[2].x, side ? u0[3].y : u0[3].x};
-                            source_terms<NF, float, false>(P, B, us, u0s, x, side ? yc2.y : yc2.x, time, dt, it);
+                            float sk1[NF], sk2[NF];
+                            euler_sink_items(P, B, us, x, side ? yc2.y : yc2.x, dt, sk1, sk2);
 #pragma unroll
                             for (int f = 0; f < NF; ++f) {
-                                const float sk = it[SINK1 * NF + f] + it[SINK2 * NF + f];
+                                const float sk = sk1[f] + sk2[f];
                                 if (side) tot[f].y += sk;
                                 else tot[f].x += sk;
-                                led1[f] += it[SINK1 * NF + f];
-                                led1[NF + f] += it[SINK2 * NF + f];
+                                led1[f] += sk1[f];
+                                led1[NF + f] += sk2[f];
                             }
                         }
                     }
@@ -570,8 +712,8 @@ stage3e_kernel(StageArgs a)
                     uo[f] = o.hi;
                 }
                 if (up_ok) {   // the same row for the whole warp
-                    const float s0 = warp_sum_items<16>(v0, lane);
-                    if (slot0 >= 0) sLed[warp][slot0] += s0;
+#pragma unroll
+                    for (int m = 0; m < 11; ++m) acc0[m] += v0[m];
                     if (sinks_any) {
                         const float s1 = warp_sum_items<8>(led1, lane);
                         if (slot1 >= 0) sLed[warp][slot1] += s1;
@@ -580,12 +722,14 @@ stage3e_kernel(StageArgs a)
                         __syncwarp();
                         sLedA[warp][lane] = sLed[warp][lane];
                         sLed[warp][lane] = 0.0f;
+                        __syncwarp();
+                        flush_acc(sLedA[warp]);
                     }
                 }
                 if (want_amax && up_ok) {
                     const float ua[NF] = {uo[0].x, uo[1].x, uo[2].x, uo[3].x};
                     const float ub[NF] = {uo[0].y, uo[1].y, uo[2].y, uo[3].y};
-                    amax = fmaxf(fmaxf(max_signal_speed<NF, float>(P, ua), max_signal_speed<NF, float>(P, ub)), amax);
+                    amax = fmaxf(fmaxf(euler_max_speed_exact(P, ua), euler_max_speed_exact(P, ub)), amax);
                 }
             }
 
@@ -627,6 +771,7 @@ stage3e_kernel(StageArgs a)
     if (t == 0 && timeout) atomicOr(a.timeout_flag, 1u);
 
     // ---- ledger pieces, one per block under the tile, each flushed by its own warp --
+    if (interior) flush_acc(sLed[warp]);   // whole warps: the main piece's group 0
     __syncthreads();
     const int brow = block / rd.nb, bcol = block - brow * rd.nb;
     const int ncol = max(TW / rd.bs, 1), wpc = TP / 32 / ncol;   // block columns; interior warps over each

@@ -96,14 +96,22 @@ def test_euler_paired_tiles_and_chunks(nb, bs, tw, rows):
     check(r)
 
 
-def test_euler_paired_tilings_match():
+TILINGS = [
+    (64, "beta_alpha", [(64, 32, 0), (64, 16, 30), (128, 32, 50), (256, 32, 0), (256, 32, 40)]),
+    (64, "torque_free", [(64, 32, 0), (128, 32, 50), (256, 32, 40)]),
+    (128, "beta_alpha", [(128, 32, 0), (256, 32, 60), (512, 32, 0), (512, 32, 100)]),
+]
+
+
+@pytest.mark.parametrize("bs,variant,tilings", TILINGS)
+def test_euler_paired_tilings_match(bs, variant, tilings):
     """Block-aligned tiles, row chunks and tiles over several block columns
-    give the same state bit for bit; ledgers and orbital elements to FP32
-    summation order."""
-    mesh, hydro, physics, model = euler_case(4, 64, variant="beta_alpha")
+    (the kernel's 128-, 256- and 512-column instantiations) give the same
+    state bit for bit; ledgers and orbital elements to FP32 summation order."""
+    mesh, hydro, physics, model = euler_case(4, bs, variant=variant)
     cons = make_case(mesh, hydro, physics, model)[0]
     out = []
-    for tw, th, rows in [(64, 32, 0), (64, 16, 30), (128, 32, 50), (256, 32, 0), (256, 32, 40)]:
+    for tw, th, rows in tilings:
         with b2.Runtime([b2.Run(mesh, hydro, physics)], precision="fp32_comp") as rt:
             rt.set_tile(tw, th)
             rt.set_strip_rows(rows)
