@@ -344,8 +344,15 @@ __global__ void __launch_bounds__(TWMAX / 2 + 32, TWMAX == 128 ? 4 : (TWMAX == 2
 #pragma unroll
     for (int f = 0; f < NF; ++f) { Pm1[f] = P0[f] = fxA[f] = fxB[f] = xg[f] = f2(0.0f); }
 
+    // row positions of the faces and updates, loaded one iteration ahead: x of
+    // row rq's zone centres (y faces), of row ru's (update), of face rq + 1/2
+    auto xc_at = [&](int r) { return xc_row[min(max(r, 0), TH - 1)]; };
+    auto xv_at = [&](int r) { return xv_row[min(max(r, 0), TH)]; };
+    float xq = xc_at(-4), xu = xc_at(-5), xvq = xv_at(-3);
+
     for (int k = 0; k < TH + 5; ++k) {
         const int rn = k - 2;
+        const float xq_next = xc_at(k - 3), xvq_next = xv_at(k - 2);
         if (producer) {
             if (rn + S3_DEPTH <= TH + 1) issue(rn + S3_DEPTH);
             const int ur = rn - 3 + S3_DEPTH;
@@ -452,7 +459,7 @@ __global__ void __launch_bounds__(TWMAX / 2 + 32, TWMAX == 128 ? 4 : (TWMAX == 2
             const float2 gl[3] = {make_float2(a0.w, b0.w), make_float2(a1.x, b1.x), make_float2(a1.y, b1.y)};
             const float2 pcr[3] = {make_float2(b0.x, d0.x), make_float2(b0.y, d0.y), make_float2(b0.z, d0.z)};
             const float2 gr[3] = {make_float2(b0.w, d0.w), make_float2(b1.x, d1.x), make_float2(b1.y, d1.y)};
-            const float x = xc_row[min(max(rq, 0), TH - 1)];
+            const float x = xq;
             const float d1x = x - B.p1.x, d2x = x - B.p2.x;
             const float2 cs2 = iso_face_cs2_2(P, B, d1x * d1x, d2x * d2x, col_part(yv2, B.p1.y), col_part(yv2, B.p2.y));
             float2 F[NF];
@@ -481,7 +488,7 @@ __global__ void __launch_bounds__(TWMAX / 2 + 32, TWMAX == 128 ? 4 : (TWMAX == 2
                 const float4 fa = frow[0], fb = frow[HF], fc = frow[1];
                 const float2 fyl[3] = {make_float2(fa.x, fb.x), make_float2(fa.y, fb.y), make_float2(fa.z, fb.z)};
                 const float2 fyr[3] = {make_float2(fb.x, fc.x), make_float2(fb.y, fc.y), make_float2(fb.z, fc.z)};
-                const float x = xc_row[rc];
+                const float x = xu;
                 if (up_ok && !mbar_wait_bounded(ubars + rc % S3_USLOTS, (rc / S3_USLOTS) & 1)) timeout = 1;
                 const float* q = (const float*)(uslots + (rc % S3_USLOTS) * USLOT);
                 float2 uc[NF], ulo[NF], u0[NF];
@@ -634,7 +641,7 @@ __global__ void __launch_bounds__(TWMAX / 2 + 32, TWMAX == 128 ? 4 : (TWMAX == 2
                 const float4 e0 = sR0[oa + HR], e1 = sR1[oa + HR], e2 = sR2[oa + HR];
                 const float2 pcl[3] = {make_float2(a0.x, e0.x), make_float2(a0.y, e0.y), make_float2(a0.z, e0.z)};
                 const float2 gl[3] = {make_float2(a2.x, e2.x), make_float2(a2.y, e2.y), make_float2(a2.z, e2.z)};
-                const float x = xv_row[min(max(rq + 1, 0), TH)];
+                const float x = xvq;
                 const float d1x = x - B.p1.x, d2x = x - B.p2.x;
                 const float2 cs2 =
                     iso_face_cs2_2(P, B, d1x * d1x, d2x * d2x, col_part(yc2, B.p1.y), col_part(yc2, B.p2.y));
@@ -646,6 +653,9 @@ __global__ void __launch_bounds__(TWMAX / 2 + 32, TWMAX == 128 ? 4 : (TWMAX == 2
 #pragma unroll
             for (int f = 0; f < NF; ++f) { fxA[f] = fxB[f]; fxB[f] = fxn[f]; }
         }
+        xu = xq;
+        xq = xq_next;
+        xvq = xvq_next;
         __syncthreads();
     }
 

@@ -434,8 +434,15 @@ stage3e_kernel(StageArgs a)
 #pragma unroll
     for (int f = 0; f < NF; ++f) { Pm1[f] = P0[f] = fxA[f] = fxB[f] = xg[f] = f2(0.0f); }
 
+    // row positions of the faces and updates, loaded one iteration ahead: x of
+    // row rq's zone centres (y faces), of row ru's (update), of face rq + 1/2
+    auto xc_at = [&](int r) { return xc_row[min(max(r, 0), TH - 1)]; };
+    auto xv_at = [&](int r) { return xv_row[min(max(r, 0), TH)]; };
+    float xq = xc_at(-4), xu = xc_at(-5), xvq = xv_at(-3);
+
     for (int k = 0; k < TH + 5; ++k) {
         const int rn = k - 2;
+        const float xq_next = xc_at(k - 3), xvq_next = xv_at(k - 2);
         if (producer) {
             if (rn + S3_DEPTH <= TH + 1) issue(rn + S3_DEPTH);
             const int ur = rn - 3 + S3_DEPTH;
@@ -548,7 +555,7 @@ stage3e_kernel(StageArgs a)
                                    make_float2(b0.w, d0.w)};
             const float2 gr[4] = {make_float2(b1.x, d1.x), make_float2(b1.y, d1.y), make_float2(b1.z, d1.z),
                                   make_float2(b1.w, d1.w)};
-            const float x = xc_row[min(max(rq, 0), TH - 1)];
+            const float x = xq;
             float2 F[NF];
             euler_face_flux2<1>(P, B, pcl, gl, make_float2(a3.x, b3.x), make_float2(a3.y, b3.y), pcr, gr,
                                 make_float2(b3.x, d3.x), make_float2(b3.y, d3.y), x, yv2, F);
@@ -575,7 +582,7 @@ stage3e_kernel(StageArgs a)
                                        make_float2(fa.w, fb.w)};
                 const float2 fyr[4] = {make_float2(fb.x, fc.x), make_float2(fb.y, fc.y), make_float2(fb.z, fc.z),
                                        make_float2(fb.w, fc.w)};
-                const float x = xc_row[rc];
+                const float x = xu;
                 if (up_ok && !mbar_wait_bounded(ubars + rc % S3_USLOTS, (rc / S3_USLOTS) & 1)) timeout = 1;
                 const float* q = (const float*)(uslots + (rc % S3_USLOTS) * USLOT);
                 float2 uc[NF], u0[NF];
@@ -744,7 +751,7 @@ stage3e_kernel(StageArgs a)
                                        make_float2(a0.w, e0.w)};
                 const float2 gl[4] = {make_float2(a2.x, e2.x), make_float2(a2.y, e2.y), make_float2(a2.z, e2.z),
                                       make_float2(a2.w, e2.w)};
-                const float x = xv_row[min(max(rq + 1, 0), TH)];
+                const float x = xvq;
                 euler_face_flux2<0>(P, B, pcl, gl, make_float2(a3.z, e3.z), make_float2(a3.y, e3.y), Pm1, xg, xtn,
                                     xtt, x, yc2, fxn);
             }
@@ -753,6 +760,9 @@ stage3e_kernel(StageArgs a)
 #pragma unroll
             for (int f = 0; f < NF; ++f) { fxA[f] = fxB[f]; fxB[f] = fxn[f]; }
         }
+        xu = xq;
+        xq = xq_next;
+        xvq = xvq_next;
         __syncthreads();
     }
 

@@ -135,9 +135,9 @@ def run_compare(args):
     res = {}
     for p in ("fp64", "fp32_comp"):
         with b2.Runtime([b2.Run(mesh, hydro, physics)], precision=p) as rt:
-            if p != "fp64":
-                rt.autotune()
             rt.upload(0, cons)
+            if p != "fp64":
+                rt.autotune()   # on the uploaded state; the trial advances are discarded
             t0 = time.time()
             for _ in range(n):
                 rt.advance(FOLD)
@@ -181,9 +181,9 @@ def run_orbit(args):
     t0 = time.time()
     status = "ok"
     with b2.Runtime([b2.Run(mesh, hydro, physics)], precision=args.precision) as rt:
-        tile = rt.autotune()
-        rows = rt.strip_rows()
         rt.upload(0, cons)
+        tile = rt.autotune()   # on the uploaded state; the trial advances are discarded
+        rows = rt.strip_rows()
         n = 0
         try:
             while rt.time(0)[0] < args.orbits * 2 * np.pi:

@@ -15,8 +15,9 @@ unused guard values to NaN.  Every case below runs in that build in a child
 process and in the normal build here: the states must be finite and equal bit
 for bit.  Cases cover every stage kernel: the generic kernel (8^2 blocks, FP64
 and FP32), the FP64 kernel on 64^2 blocks, the TMA-staged kernel (32-column
-tiles, Euler, FP64 state), and the paired kernel (64-, 128- and 512-column
-tiles, row chunks)."""
+tiles, Euler, FP64 state), the paired isothermal kernel (64-, 128- and
+512-column tiles, row chunks) and the paired Euler kernel (64-, 256- and
+512-column tiles, row chunks)."""
 import json
 import os
 import subprocess
@@ -35,11 +36,14 @@ CASES = {
     "generic_fp32_8": ("iso", 4, 8, "fp32_comp", None, 0),
     "fp64_64": ("iso", 4, 64, "fp64", None, 0),
     "staged_32": ("iso", 4, 64, "fp32_comp", (32, 32), 0),
-    "staged_euler_64": ("euler", 4, 64, "fp32_comp", (64, 32), 40),
+    "staged_euler_32": ("euler", 4, 64, "fp32_comp", (32, 32), 40),
     "staged_state64_64": ("iso", 4, 64, "fp32_state64", (64, 32), 0),
     "paired_64": ("iso", 4, 64, "fp32_comp", (64, 32), 0),
     "paired_128_chunks": ("iso", 4, 64, "fp32_comp", (128, 32), 50),
     "paired_512_chunks": ("iso", 4, 128, "fp32_comp", (512, 32), 100),
+    "paired_euler_64": ("euler", 4, 64, "fp32_comp", (64, 32), 40),
+    "paired_euler_256_chunks": ("euler", 4, 128, "fp32_comp", (256, 32), 60),
+    "paired_euler_512_chunks": ("euler", 4, 128, "fp32_comp", (512, 32), 100),
 }
 
 RUNNER = r"""
