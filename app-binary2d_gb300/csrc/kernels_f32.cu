@@ -42,7 +42,7 @@ static cudaError_t launch_three_impl(const StageArgs& a, int grid, int tw, cudaS
     size_t smem = s3_smem_bytes(tw);
     cudaError_t e = opt_in_smem((const void*)k, smem);
     if (e != cudaSuccess) return e;
-    k<<<grid, tw / 2 + 32, smem, s>>>(a);
+    k<<<grid, tw / 2 + 32 * s3_aux_warps(TWMAX), smem, s>>>(a);
     return cudaGetLastError();
 }
 
@@ -72,7 +72,7 @@ int stage_ctas_per_sm(int nf, int store, int nruns, int tw)
         else k = nruns == 1 ? stage3_kernel<true, 512> : stage3_kernel<false, 512>;
         // the opt-in above 48 KB of dynamic shared memory, as at launch
         if (opt_in_smem((const void*)k, smem) != cudaSuccess) return 0;
-        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, tw / 2 + 32, smem);
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, tw / 2 + 32 * s3_aux_warps(tw <= 128 ? 128 : tw), smem);
         return e == cudaSuccess ? n : 0;
     }
     if (tw % 32 == 0 && tw <= 128) {

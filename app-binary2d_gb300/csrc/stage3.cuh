@@ -18,9 +18,10 @@
 //  * Exchange.  A pair needs its left neighbour's column for the y-slopes and
 //    the face at 2t, and its right neighbour's first y-flux; both go through
 //    float4 planes in shared memory as in stage2.
-//  * Halo.  A fifth warp owns the guard pairs (-2, -1) and (TW, TW+1) on lanes
+//  * Halo.  An extra warp owns the guard pairs (-2, -1) and (TW, TW+1) on lanes
 //    0 and 1 (lane 1 also computes the y-faces at TW and TW+1, of which TW is
-//    the tile's right face) and the TMA producer on lane 4.  The halo lanes'
+//    the tile's right face); the TMA producer is its lane 4 on 64- and
+//    128-column tiles and lane 0 of a second extra warp on wider ones.  The halo lanes'
 //    outer columns (-2 and TW+1) need stencil points outside the staged halo;
 //    they read clamped in-bounds values and their results are never used.
 //  * Row chunks.  A tile is a column strip's row chunk (chunk_start,
@@ -168,19 +169,34 @@ __host__ __device__ inline int s3_smem_bytes(int tw)
     return slots + exch + 8 * (S3_SLOTS + S3_USLOTS);
 }
 
+// Warps beside the interior ones: the halo warp, and for 256- and 512-column
+// tiles a warp of its own for the TMA producer (lane 0), so that the bulk-copy
+// issue of a row does not add to the halo warp's time on its sub-partition
+// (measured on the 2048^2 disk: 0.1320 against 0.1347 ms per stage at
+// 512-column tiles).  Launch: TW / 2 + 32 * s3_aux_warps threads.
+__host__ __device__ constexpr int s3_aux_warps(int twmax) { return twmax >= 256 ? 2 : 1; }
+// The launch bound's thread count: the CTA's threads, except that the
+// 512-column CTA (10 warps, 3 on some sub-partition) is declared as 384
+// threads, which caps a thread at 168 registers as three warps on one
+// sub-partition require.
+__host__ __device__ constexpr int s3_launch_bound(int twmax)
+{
+    return twmax == 512 ? 384 : twmax / 2 + 32 * s3_aux_warps(twmax);
+}
+
 // TWMAX: the widest tile of the instantiation.  128: tiles of 64 or 128
 // columns, 4 CTAs per SM; 256: 256-column tiles over two 128-column blocks
 // (or one 256-column block), 4 interior warps to each halo warp, 2 CTAs per
 // SM; 512: 512-column tiles over up to four blocks, 8 interior warps to each
 // halo warp, 1 CTA per SM.
 template <bool SINGLE, int TWMAX>
-__global__ void __launch_bounds__(TWMAX / 2 + 32, TWMAX == 128 ? 4 : (TWMAX == 256 ? 2 : 1)) stage3_kernel(StageArgs a)
+__global__ void __launch_bounds__(s3_launch_bound(TWMAX), TWMAX == 128 ? 4 : (TWMAX == 256 ? 2 : 1)) stage3_kernel(StageArgs a)
 {
     constexpr int NF = 3;
     constexpr int H = 4;                     // staged halo columns per side: 16 bytes of FP32
     constexpr int NL = NITEMS * NF;
 
-    const int TP = blockDim.x - 32;          // interior threads (column pairs)
+    const int TP = blockDim.x - 32 * s3_aux_warps(TWMAX);   // interior threads (column pairs)
     const int TW = 2 * TP;
     const int t = threadIdx.x;
     const int SW = TW + 2 * H;
@@ -255,10 +271,10 @@ __global__ void __launch_bounds__(TWMAX / 2 + 32, TWMAX == 128 ? 4 : (TWMAX == 2
 
     // ---- roles -----------------------------------------------------------------
     const bool interior = t < TP;
-    const int hl = t - TP;                                    // lane in the halo warp
+    const int hl = t - TP;                                    // lane in the halo warp (32: the producer warp)
     const bool active = interior || (hl >= 0 && hl < 2);
     const int c0 = interior ? 2 * t : (hl == 0 ? -2 : TW);   // first column of this thread's pair
-    const bool producer = (hl == 4);
+    const bool producer = s3_aux_warps(TWMAX) == 2 ? hl == 32 : hl == 4;
     const int p = c0 >> 1;                                   // the pair's slot in a half row (-1 for the -2 pair)
     const int HR = TW / 2 + 2, HF = TW / 2 + 1;              // odd halves of the record and flux rows
 
