@@ -375,6 +375,12 @@ __global__ void __launch_bounds__(s3_launch_bound(TWMAX), TWMAX == 128 ? 4 : (TW
             if (ur >= 0 && ur <= TH - 1) issue_update(ur);
         }
 
+        // the update ring's row rn - 3, waited for before the row's work so that
+        // the update below runs without a wait inside it
+        if (interior && rn >= 3 && rn - 3 <= TH - 1 &&
+            !mbar_wait_bounded(ubars + (rn - 3) % S3_USLOTS, ((rn - 3) / S3_USLOTS) & 1))
+            timeout = 1;
+
         // ---- phase 1: row rn -> primitives (try_block_primitive, scheme.rs:185-199) --
         float2 pn[NF];
 #pragma unroll
@@ -491,10 +497,14 @@ __global__ void __launch_bounds__(s3_launch_bound(TWMAX), TWMAX == 128 ? 4 : (TW
             }
         };
         float2 fxn[NF];
-        // one call site for the y faces (the halo lane of the tile's right face
-        // included): the kernel's code is smaller (measured 2 % faster)
-        if ((interior && rn >= 1) || (hl == 1 && fy_ok)) y_flux();
+        // The y fluxes, the update and the x fluxes of an interior pair in one
+        // block without a wait (the update ring's row is waited for before
+        // phase 1), so that the compiler can interleave their independent
+        // chains; the halo lane of the tile's right face computes its y fluxes
+        // apart (measured on the 2048^2 disk: 0.1273 ms per stage against
+        // 0.1321 with one call site for both and the wait inside the update).
         if (interior && rn >= 1) {
+            y_flux();
 
             // update of row ru
             {
@@ -505,7 +515,6 @@ __global__ void __launch_bounds__(s3_launch_bound(TWMAX), TWMAX == 128 ? 4 : (TW
                 const float2 fyl[3] = {make_float2(fa.x, fb.x), make_float2(fa.y, fb.y), make_float2(fa.z, fb.z)};
                 const float2 fyr[3] = {make_float2(fb.x, fc.x), make_float2(fb.y, fc.y), make_float2(fb.z, fc.z)};
                 const float x = xu;
-                if (up_ok && !mbar_wait_bounded(ubars + rc % S3_USLOTS, (rc / S3_USLOTS) & 1)) timeout = 1;
                 const float* q = (const float*)(uslots + (rc % S3_USLOTS) * USLOT);
                 float2 uc[NF], ulo[NF], u0[NF];
 #pragma unroll
@@ -664,6 +673,8 @@ __global__ void __launch_bounds__(s3_launch_bound(TWMAX), TWMAX == 128 ? 4 : (TW
                 face_flux2<0>(P, B, pcl, gl, make_float2(a2.w, e2.w), make_float2(a1.w, e1.w), Pm1, xg, xtn, xtt,
                               f2(x), yc2, cs2, fxn);
             }
+        } else if (hl == 1 && fy_ok) {
+            y_flux();
         }
         if (fx_ok) {
 #pragma unroll
