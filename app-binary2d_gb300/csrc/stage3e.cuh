@@ -348,7 +348,13 @@ stage3e_kernel(StageArgs a)
             bulk_load(dst, row + j0, TW * sizeof(float), bar);
         } else if (j0 >= H && j0 + TW + H <= N) {
             bulk_load(dst, row + j0 - H, SW * sizeof(float), bar);
-        } else {
+        } else if (j0 == 0 && TW + H <= N) {   // the mesh's left edge: the left halo wraps to the row's end
+            bulk_load(dst, row + N - H, H * sizeof(float), bar);
+            bulk_load(dst + H * sizeof(float), row, (TW + H) * sizeof(float), bar);
+        } else if (j0 >= H) {                  // the right edge (j0 + TW = N): the right halo wraps to column 0
+            bulk_load(dst, row + j0 - H, (TW + H) * sizeof(float), bar);
+            bulk_load(dst + (TW + H) * sizeof(float), row, H * sizeof(float), bar);
+        } else {                               // one strip spans the row: both halos wrap
             bulk_load(dst, row + (j0 - H + N) % N, H * sizeof(float), bar);
             bulk_load(dst + H * sizeof(float), row + j0, TW * sizeof(float), bar);
             bulk_load(dst + (H + TW) * sizeof(float), row + (j0 + TW) % N, H * sizeof(float), bar);
