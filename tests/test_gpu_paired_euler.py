@@ -159,3 +159,32 @@ def test_euler_preset_block_on_the_paired_kernel():
     r = run_pair(mesh, hydro, physics, model, fold=10, advances=2, precision="fp32_comp", tile=(512, 32),
                  strip_rows=100)
     check(r)
+
+
+@pytest.mark.parametrize("kind", ["NegativePressure", "NegativeDensity"])
+def test_euler_paired_failure_reports_the_zone(kind):
+    """Euler::try_to_primitive's errors (physics.rs:631-660) from the paired
+    kernel: the advance fails with the zone and the kind, and the context
+    keeps the pre-advance state (main.rs:159-205)."""
+    mesh, hydro, physics, model = euler_case(4, 64, variant="t4")
+    cons, cfg = make_case(mesh, hydro, physics, model)
+    bad = cons.copy()
+    z = bad[2, 3, 17, 40]
+    if kind == "NegativePressure":
+        z[3] = 0.5 * (z[1] ** 2 + z[2] ** 2) / z[0] - 1.0     # E below the kinetic energy
+    else:
+        z[0] = -1e-3
+    with b2.Runtime([b2.Run(mesh, hydro, physics)], precision="fp32_comp") as rt:
+        rt.set_tile(128, 32)
+        rt.set_strip_rows(50)
+        rt.upload(0, bad, background=cons, time=0.5, iteration=3)
+        with pytest.raises(b2.HydroError) as ei:
+            rt.advance(2)
+        e = ei.value
+        assert e.kind == kind
+        assert e.block == (2, 3) and e.zone == (17, 40)
+        out, t, it = rt.download(0)
+        assert np.allclose(out, bad, rtol=1e-14, atol=0) and t == 0.5 and it == 3
+        ref = binding.OracleState(cfg, bad, background=cons)
+        with pytest.raises(binding.OracleHydroError):
+            ref.advance(2)
