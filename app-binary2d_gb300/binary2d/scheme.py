@@ -239,7 +239,8 @@ class Runtime:
     # -- row slabs (one run split across contexts) ------------------------------
     def set_slab(self, run: int, block_row_lo: int, block_row_hi: int):
         """Make block rows [lo, hi) of `run` this context's slab ((0, 0): the
-        whole run); FP64 precision only."""
+        whole run).  A slab's stage launches cover its block-aligned tiles of
+        the tile height (row chunks apply to whole runs only)."""
         _check(self.lib.b2d_set_slab(self.ctx, run, int(block_row_lo), int(block_row_hi)))
 
     def slab_begin(self, fold: int, amax):
@@ -261,16 +262,22 @@ class Runtime:
         return dts
 
     def slab_rows(self, run: int, row0: int, nrows: int) -> np.ndarray:
-        """Zone rows [row0, row0 + nrows) (periodic) of the next stage's input:
-        [nf, nrows, N] FP64."""
+        """Zone rows [row0, row0 + nrows) (periodic) of the next stage's input,
+        as stored: [nf, nrows, N] FP64, or for the compensated FP32 state
+        [nf, 2, nrows, N] FP32 (hi and lo words)."""
         N = self.runs[run].mesh.zones_per_side()
-        out = np.empty((self.nf, nrows, N), dtype=np.float64)
-        _check(self.lib.b2d_slab_rows(self.ctx, run, int(row0), int(nrows), _dp(out), 0))
+        if self.precision == "fp32_comp":
+            out = np.empty((self.nf, 2, nrows, N), dtype=np.float32)
+        else:
+            out = np.empty((self.nf, nrows, N), dtype=np.float64)
+        _check(self.lib.b2d_slab_rows(self.ctx, run, int(row0), int(nrows), out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), 0))
         return out
 
     def put_slab_rows(self, run: int, row0: int, rows: np.ndarray):
-        r = np.ascontiguousarray(rows, dtype=np.float64)
-        _check(self.lib.b2d_slab_rows(self.ctx, run, int(row0), r.shape[1], _dp(r), 1))
+        """Write rows got from slab_rows of a context of the same precision."""
+        dtype = np.float32 if self.precision == "fp32_comp" else np.float64
+        r = np.ascontiguousarray(rows, dtype=dtype)
+        _check(self.lib.b2d_slab_rows(self.ctx, run, int(row0), r.shape[-2], r.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), 1))
 
     # -- tuning / introspection ----------------------------------------------
     def set_tile(self, w: int = 0, h: int = 0):

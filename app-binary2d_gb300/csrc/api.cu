@@ -491,7 +491,10 @@ static b2d_status sync_rundev(b2d_ctx* ctx)
     for (int i = 0; i < ctx->nruns; ++i) {
         RunHost& r = ctx->runs[i];
         RunDev& d = ctx->rdev_h[i];
-        d.tiles_i = d.slab_hi > 0 ? (d.slab_hi - d.slab_lo) * (r.bs / ctx->th) : row_chunks(ctx, r);
+        // a slab launches the block-aligned chunks (tile height th) of its own block rows
+        d.chunks = d.slab_hi > 0 ? r.N / ctx->th : row_chunks(ctx, r);
+        d.chunk0 = d.slab_hi > 0 ? d.slab_lo * (r.bs / ctx->th) : 0;
+        d.tiles_i = d.slab_hi > 0 ? (d.slab_hi - d.slab_lo) * (r.bs / ctx->th) : d.chunks;
         d.tiles_j = r.N / ctx->tw;
         d.ntiles = d.tiles_i * d.tiles_j;
         d.tile_base = base;
@@ -500,7 +503,7 @@ static b2d_status sync_rundev(b2d_ctx* ctx)
         int most = 0;
         if (d.slab_hi > 0) most = r.bs / ctx->th;   // a slab's tiles are block-aligned
         else
-            for (int b = 0; b < r.nb; ++b) most = std::max(most, chunks_in_block_row(b, r.bs, r.N, d.tiles_i));
+            for (int b = 0; b < r.nb; ++b) most = std::max(most, chunks_in_block_row(b, r.bs, r.N, d.chunks));
         d.tiles_per_block = most * std::max(r.bs / ctx->tw, 1);
         base += d.ntiles;
         CUDA_TRY(cudaFree(r.partial));
@@ -1721,8 +1724,6 @@ extern "C" b2d_status b2d_set_slab(b2d_ctx* ctx, int32_t run, int32_t block_row_
     const bool whole = block_row_lo == 0 && block_row_hi == 0;
     if (!whole && (block_row_lo < 0 || block_row_hi > d.nb || block_row_lo >= block_row_hi))
         return fail(B2D_ERR_INVALID, "slab rows must satisfy 0 <= lo < hi <= num_blocks");
-    if (!whole && ctx->precision != B2D_PREC_FP64)
-        return fail(B2D_ERR_UNSUPPORTED, "row slabs run on the FP64 kernel (block-aligned tiles) only");
     CUDA_TRY(cudaStreamSynchronize(ctx->stream));
     d.slab_lo = whole ? 0 : block_row_lo;
     d.slab_hi = whole ? 0 : block_row_hi;
@@ -1788,22 +1789,28 @@ extern "C" b2d_status b2d_slab_end(b2d_ctx* ctx, double* dt_out, b2d_error* err_
 extern "C" b2d_status b2d_slab_rows(b2d_ctx* ctx, int32_t run, int32_t row0, int32_t nrows, double* rows, int32_t put)
 {
     if (!ctx || run < 0 || run >= ctx->nruns || !rows || nrows < 1) return fail(B2D_ERR_INVALID, "bad arguments");
-    if (ctx->precision != B2D_PREC_FP64) return fail(B2D_ERR_UNSUPPORTED, "row exchange of the FP64 state only");
     RunHost& r = ctx->runs[run];
     if (nrows > r.N) return fail(B2D_ERR_INVALID, "more rows than the mesh has");
     // the next stage's input slot, or the current state between advances
     const int slot = ctx->slab_next >= 0 && ctx->slab_next < (int)ctx->slab_plan.size()
                          ? ctx->slab_plan[ctx->slab_next].in : ctx->cur;
     const size_t nn = (size_t)r.N * r.N;
-    double* planes = (double*)r.slot[slot];
+    // the stored words as they are: FP64 planes (FP64 and FP64-state contexts),
+    // or the hi and lo FP32 planes of the compensated state, so that the
+    // receiving context continues with exactly the sender's words
+    const int parts = store_of(ctx) == 1 ? 2 : 1;
+    const size_t w = store_of(ctx) == 1 ? sizeof(float) : sizeof(double);
+    unsigned char* planes = (unsigned char*)r.slot[slot];
+    unsigned char* buf = (unsigned char*)rows;
     for (int f = 0; f < ctx->nf; ++f)
-        for (int k = 0; k < nrows; ++k) {
-            const int gi = ((row0 + k) % r.N + r.N) % r.N;
-            double* dev = planes + f * nn + (size_t)gi * r.N;
-            double* host = rows + ((size_t)f * nrows + k) * r.N;
-            if (put) CUDA_TRY(cudaMemcpyAsync(dev, host, sizeof(double) * r.N, cudaMemcpyHostToDevice, ctx->stream));
-            else CUDA_TRY(cudaMemcpyAsync(host, dev, sizeof(double) * r.N, cudaMemcpyDeviceToHost, ctx->stream));
-        }
+        for (int part = 0; part < parts; ++part)
+            for (int k = 0; k < nrows; ++k) {
+                const int gi = ((row0 + k) % r.N + r.N) % r.N;
+                unsigned char* dev = planes + (((size_t)(f * parts + part)) * nn + (size_t)gi * r.N) * w;
+                unsigned char* host = buf + (((size_t)(f * parts + part) * nrows + k) * r.N) * w;
+                if (put) CUDA_TRY(cudaMemcpyAsync(dev, host, w * r.N, cudaMemcpyHostToDevice, ctx->stream));
+                else CUDA_TRY(cudaMemcpyAsync(host, dev, w * r.N, cudaMemcpyDeviceToHost, ctx->stream));
+            }
     CUDA_TRY(cudaStreamSynchronize(ctx->stream));
     return B2D_OK;
 }
@@ -1923,6 +1930,7 @@ extern "C" b2d_status b2d_stage_noalloc(const b2d_config* cfg, const double* d_i
     memset(&rd, 0, sizeof rd);
     rd.N = N; rd.bs = bs; rd.nb = nb; rd.nblocks = nblocks;
     rd.tiles_i = N / th; rd.tiles_j = N / tw; rd.ntiles = ntiles; rd.tile_base = 0;
+    rd.chunks = rd.tiles_i; rd.chunk0 = 0;
     rd.tiles_per_block = tiles_per_block;
     rd.xc = d_xc; rd.xv = d_xv;
     rd.slot[0] = (void*)d_in; rd.slot[1] = (void*)d_base; rd.slot[2] = d_out; rd.slot[3] = d_out;

@@ -14,10 +14,13 @@ struct df32w { float hi, lo; };
 struct RunDev {
     int N, bs, nb, nblocks;
     int tiles_i, tiles_j, ntiles, tile_base;
-    int tiles_per_block, pad_;   // partial slots per block: the most ledger pieces a block receives
+    int tiles_per_block, chunk0; // partial slots per block: the most ledger pieces a block receives;
+                                 // the first row chunk the launch covers (a slab's; 0 for the whole run)
     int slab_lo, slab_hi;        // row slab: block rows [slab_lo, slab_hi) of the run are this context's
                                  // (slab_hi = 0: the whole run); the stage kernel's tiles, the max
                                  // speed and the orbital-element ledger cover only the slab
+    int chunks, pad_;            // row chunks per column strip of the whole run (C of chunk_start);
+                                 // tiles_i of them, from chunk0, are launched
     const double* xc;        // [N] cell centres by global index (block formula, mesh.rs:49-54)
     const double* xv;        // [nb][bs+1] block vertices (mesh.rs:42-47)
     const float* xcf;

@@ -278,8 +278,8 @@ __device__ __noinline__ void flush_piece(const RunDev& rd, int brow, int bj, int
         if (slot0 >= 0) bank[0][slot0] += s0;
         __syncwarp();
     }
-    const int bs = rd.bs, nc = rd.tiles_i, per_row = max(bs / TW, 1);
-    const int ti = ((int)blockIdx.x - rd.tile_base) / rd.tiles_j;
+    const int bs = rd.bs, nc = rd.chunks, per_row = max(bs / TW, 1);
+    const int ti = rd.chunk0 + ((int)blockIdx.x - rd.tile_base) / rd.tiles_j;
     const int block = brow * rd.nb + bj;
     const int piece = (ti - chunk_of_row(brow * bs, rd.N, nc)) * per_row + lslot;
     const int pieces = chunks_in_block_row(brow, bs, rd.N, nc) * per_row;
@@ -359,11 +359,11 @@ __global__ void __launch_bounds__(160, (NF == 3 && STORE == 1) ? 4 : 3) stage2_k
     const int N = rd.N, bs = rd.bs;
     const size_t nn = (size_t)N * N;
     const int lt = g - rd.tile_base;
-    const int tj = lt % rd.tiles_j, ti = lt / rd.tiles_j;
+    const int tj = lt % rd.tiles_j, ti = rd.chunk0 + lt / rd.tiles_j;
     // rows [i0, i0 + TH): row chunk ti of C (chunk_start, runtime.cuh); a chunk
     // of at most bs rows lies in one block row, or in two from its row rb, and
     // its ledger piece in the last of them is the tile's main piece
-    const int C = rd.tiles_i;
+    const int C = rd.chunks;
     const int i0 = chunk_start(ti, N, C), TH = chunk_start(ti + 1, N, C) - i0, j0 = tj * TW;
     const int bj = j0 / bs, lj0 = j0 % bs;
     const int rb = min(bs - i0 % bs, TH);

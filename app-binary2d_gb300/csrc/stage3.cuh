@@ -229,11 +229,11 @@ __global__ void __launch_bounds__(s3_launch_bound(TWMAX), TWMAX == 128 ? 4 : (TW
     const int N = rd.N, bs = rd.bs;
     const size_t nn = (size_t)N * N;
     const int lt = g - rd.tile_base;
-    const int tj = lt % rd.tiles_j, ti = lt / rd.tiles_j;
+    const int tj = lt % rd.tiles_j, ti = rd.chunk0 + lt / rd.tiles_j;
     // rows [i0, i0 + TH) of the column strip from j0: row chunk ti of C.  A chunk
     // of at most bs rows lies in one block row, or in two from its row rb; the
     // ledger piece of the last block row is the tile's main piece
-    const int C = rd.tiles_i;
+    const int C = rd.chunks;
     const int i0 = chunk_start(ti, N, C), TH = chunk_start(ti + 1, N, C) - i0, j0 = tj * TW;
     const int bj = j0 / bs, lj0 = j0 % bs;
     const int rb = min(bs - i0 % bs, TH);

@@ -296,9 +296,9 @@ stage3e_kernel(StageArgs a)
     const int N = rd.N, bs = rd.bs;
     const size_t nn = (size_t)N * N;
     const int lt = g - rd.tile_base;
-    const int tj = lt % rd.tiles_j, ti = lt / rd.tiles_j;
+    const int tj = lt % rd.tiles_j, ti = rd.chunk0 + lt / rd.tiles_j;
     // rows [i0, i0 + TH) of the column strip from j0: row chunk ti of C (as in stage3.cuh)
-    const int C = rd.tiles_i;
+    const int C = rd.chunks;
     const int i0 = chunk_start(ti, N, C), TH = chunk_start(ti + 1, N, C) - i0, j0 = tj * TW;
     const int bj = j0 / bs, lj0 = j0 % bs;
     const int rb = min(bs - i0 % bs, TH);

@@ -361,8 +361,9 @@ b2d_status b2d_set_device(int32_t device);
  *      errors as b2d_advance reports them.
  * The per-block ledgers of the slab's blocks are this context's; a caller
  * sums them with the other slabs' (each block has one owner).  The results
- * equal an unsplit run's bit for bit.  FP64 precision only (block-aligned
- * tiles of the FP64 kernel). */
+ * equal an unsplit run's with the same block-aligned tiles bit for bit, at
+ * every precision (a slab's stage launches cover its block-aligned tiles of
+ * the tile height; row chunks apply to whole runs only). */
 
 /* Make block rows [block_row_lo, block_row_hi) of `run` this context's slab
  * ((0, 0): the whole run again).  The stage kernel then covers only the
@@ -383,7 +384,10 @@ b2d_status b2d_slab_end(b2d_ctx* ctx, double* dt_out, b2d_error* err_out);
 
 /* Copy zone rows [row0, row0 + nrows) (periodic) of the next stage's input
  * (between advances: of the current state) to (put = 0) or from (put = 1)
- * `rows`, laid out [nf][nrows][N] in FP64. */
+ * `rows`, as stored: [nf][nrows][N] FP64 words (FP64 and FP64-state
+ * contexts) or [nf][2][nrows][N] FP32 words, hi then lo (compensated FP32
+ * state); either is nf * nrows * N * 8 bytes.  Rows got from one context
+ * are put into another of the same precision. */
 b2d_status b2d_slab_rows(b2d_ctx* ctx, int32_t run, int32_t row0, int32_t nrows, double* rows, int32_t put);
 
 /* ------------------------------------------------------------------------ */

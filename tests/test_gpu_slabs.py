@@ -1,6 +1,7 @@
 """One run split into row slabs across contexts on one GPU, against the
-unsplit run: bit-identical states, per-block ledgers and orbital-element
-changes, and the same dt every advance.
+unsplit run with the same block-aligned tiles: bit-identical states,
+per-block ledgers and orbital-element changes, and the same dt every advance,
+on the FP64 kernel and on the FP32 kernels (compensated and FP64 state).
 
 Each context owns a slab of block rows (b2d_set_slab).  Per advance: the
 slabs' maximum signal speeds are reduced with max and passed to
@@ -24,12 +25,12 @@ def slabs_of(nb, k):
     return [(r * nb // k, (r + 1) * nb // k) for r in range(k)]
 
 
-def split_run(mesh, hydro, physics, cons, nslab, fold, advances, tile):
+def split_run(mesh, hydro, physics, cons, nslab, fold, advances, tile, precision="fp64"):
     bs, N = mesh.block_size, mesh.zones_per_side()
     parts = slabs_of(mesh.num_blocks, nslab)
     rts = []
     for lo, hi in parts:
-        rt = b2.Runtime([b2.Run(mesh, hydro, physics)], precision="fp64")
+        rt = b2.Runtime([b2.Run(mesh, hydro, physics)], precision=precision)
         rt.set_tile(*tile)
         rt.upload(0, cons)
         rt.set_slab(0, lo, hi)
@@ -66,13 +67,22 @@ def split_run(mesh, hydro, physics, cons, nslab, fold, advances, tile):
     return state, led, el, dts, t_end[0]
 
 
-@pytest.mark.parametrize("nb,bs,nslab,tile,variant", [
-    (4, 32, 2, (32, 16), "iso"),
-    (6, 32, 3, (32, 32), "iso"),
-    (4, 64, 2, (64, 32), "alpha_rk3"),
-    (4, 32, 2, (32, 16), "euler"),
+@pytest.mark.parametrize("nb,bs,nslab,tile,variant,precision", [
+    (4, 32, 2, (32, 16), "iso", "fp64"),
+    (6, 32, 3, (32, 32), "iso", "fp64"),
+    (4, 64, 2, (64, 32), "alpha_rk3", "fp64"),
+    (4, 32, 2, (32, 16), "euler", "fp64"),
+    # the FP32 kernels on slabs: paired isothermal (64- and 512-column tiles),
+    # paired Euler, the one-column kernel on compensated and on FP64 state
+    (4, 64, 2, (64, 32), "iso", "fp32_comp"),
+    (4, 128, 2, (512, 32), "iso", "fp32_comp"),
+    (6, 64, 3, (128, 16), "alpha_rk3", "fp32_comp"),
+    (4, 64, 2, (64, 32), "euler", "fp32_comp"),
+    (4, 128, 2, (512, 64), "euler", "fp32_comp"),
+    (4, 32, 2, (32, 16), "iso", "fp32_comp"),
+    (4, 64, 2, (64, 32), "euler", "fp32_state64"),
 ])
-def test_slabs_match_the_whole_run(nb, bs, nslab, tile, variant):
+def test_slabs_match_the_whole_run(nb, bs, nslab, tile, variant, precision):
     import dataclasses
     mesh, hydro, physics, model = b2.presets.iso_disk(nb, bs, seed=96)
     if variant == "alpha_rk3":
@@ -83,8 +93,8 @@ def test_slabs_match_the_whole_run(nb, bs, nslab, tile, variant):
         model = b2.DiskModel(surface_density=1.0, mach_number=5.0, noise=1e-3, seed=5)
     cons = make_case(mesh, hydro, physics, model)[0]
     fold, advances = 2, 3
-    state, led, el, dts, (t, it) = split_run(mesh, hydro, physics, cons, nslab, fold, advances, tile)
-    with b2.Runtime([b2.Run(mesh, hydro, physics)], precision="fp64") as rt:
+    state, led, el, dts, (t, it) = split_run(mesh, hydro, physics, cons, nslab, fold, advances, tile, precision)
+    with b2.Runtime([b2.Run(mesh, hydro, physics)], precision=precision) as rt:
         rt.set_tile(*tile)
         rt.upload(0, cons)
         ref_dts = [rt.advance(fold)[0] for _ in range(advances)]
@@ -114,5 +124,8 @@ def test_slab_arguments():
         rt.set_slab(0, 1, 3)
         assert rt.max_signal_speed(0) <= whole_max
     with b2.Runtime([b2.Run(mesh, hydro, physics)], precision="fp32_comp") as rt:
-        with pytest.raises(b2.B2DException):
-            rt.set_slab(0, 0, 2)
+        rt.upload(0, cons)
+        rt.set_slab(0, 0, 2)             # every precision takes slabs
+        got = rt.slab_rows(0, 62, 4)     # the compensated state's hi and lo words
+        assert got.dtype == np.float32 and got.shape == (3, 2, 4, 128)
+        rt.put_slab_rows(0, 62, got)
