@@ -6,7 +6,7 @@
 // intercell_flux 776-803, source_terms 683-774; the RK average of
 // state.rs:183-199) on the thread mapping of stage3.cuh: column pairs in
 // float2 registers, the TMA row ring, the halo warp (lanes 0 and 1 own the
-// guard pairs, lane 4 the producer), row chunks across one block row and
+// guard pairs, lane 4 the producer), row chunks that cross at most one block boundary, and
 // tiles across block columns.  What the fourth field changes:
 //
 //  * Cell records take four float4 planes: pc | gy | gx | (tyy, txy, txx).
